@@ -1,0 +1,159 @@
+"""ctypes view of the libfauxglcuda C ABI (include/fauxglcuda.h).
+
+The structs here are the exact layouts of fgc_state, fgc_shader and
+fgc_rasterize_info. Loading the library fails loudly when it has not been
+built: there is no CPU fallback for any drawing call.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libfauxglcuda.so")
+
+FGC_OK = 0
+FGC_ERR_INVALID_ARGUMENT = 1
+FGC_ERR_UNSUPPORTED_SHADER = 2
+FGC_ERR_CUDA = 3
+FGC_ERR_OUT_OF_MEMORY = 4
+FGC_ERR_DEVICE_LIMIT = 5
+FGC_ERR_UNSUPPORTED = 6
+
+FGC_FACE_CW = 1
+FGC_FACE_CCW = 2
+FGC_CULL_NONE = 1
+FGC_CULL_FRONT = 2
+FGC_CULL_BACK = 3
+FGC_SHADER_SOLID_COLOR = 1
+FGC_SHADER_TEXTURE = 2
+FGC_SHADER_PHONG = 3
+FGC_PRECISION_PLAIN = 0
+FGC_PRECISION_MIXED = 1
+FGC_DEBUG_WINNER = 1
+FGC_DEBUG_SHADED_COLOR = 2
+
+
+class FgcRasterizeInfo(ctypes.Structure):
+    _fields_ = [("total_pixels", ctypes.c_uint64), ("updated_pixels", ctypes.c_uint64)]
+
+
+class FgcState(ctypes.Structure):
+    _fields_ = [
+        ("read_depth", ctypes.c_int32),
+        ("write_depth", ctypes.c_int32),
+        ("write_color", ctypes.c_int32),
+        ("alpha_blend", ctypes.c_int32),
+        ("wireframe", ctypes.c_int32),
+        ("front_face", ctypes.c_int32),
+        ("cull", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("line_width", ctypes.c_double),
+        ("depth_bias", ctypes.c_double),
+    ]
+
+
+class FgcShader(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("matrix", ctypes.c_double * 16),
+        ("color", ctypes.c_double * 4),
+        ("light_direction", ctypes.c_double * 3),
+        ("camera_position", ctypes.c_double * 3),
+        ("ambient_color", ctypes.c_double * 4),
+        ("diffuse_color", ctypes.c_double * 4),
+        ("specular_color", ctypes.c_double * 4),
+        ("specular_power", ctypes.c_double),
+        ("texture", ctypes.c_void_p),
+    ]
+
+
+# Every exported symbol of include/fauxglcuda.h, with (restype, argtypes).
+_P = ctypes.c_void_p
+_PP = ctypes.POINTER(ctypes.c_void_p)
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.c_int
+_I32 = ctypes.c_int32
+_U64 = ctypes.c_uint64
+_ST = ctypes.POINTER(FgcState)
+_SH = ctypes.POINTER(FgcShader)
+_INFO = ctypes.POINTER(FgcRasterizeInfo)
+
+SIGNATURES = {
+    "fgc_abi_version": (_I32, []),
+    "fgc_state_default": (None, [_ST]),
+    "fgc_shader_solid_color": (None, [_SH, _D, _D]),
+    "fgc_shader_texture": (None, [_SH, _D, _P]),
+    "fgc_shader_phong": (None, [_SH, _D, _D, _D]),
+    "fgc_last_error": (ctypes.c_char_p, []),
+    "fgc_context_create": (_I, [_I32, _I32, _PP]),
+    "fgc_context_destroy": (_I, [_P]),
+    "fgc_context_size": (_I, [_P, ctypes.POINTER(_I32), ctypes.POINTER(_I32)]),
+    "fgc_context_set_debug": (_I, [_P, _I32]),
+    "fgc_clear_color": (_I, [_P, _D]),
+    "fgc_clear_depth": (_I, [_P, ctypes.c_double]),
+    "fgc_mesh_upload": (_I, [_D, _D, _D, _D, _U64, _D, _D, _D, _D, _U64, _PP]),
+    "fgc_mesh_release": (_I, [_P]),
+    "fgc_mesh_counts": (_I, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
+    "fgc_texture_upload": (_I, [ctypes.POINTER(ctypes.c_uint16), _I32, _I32, _PP]),
+    "fgc_texture_release": (_I, [_P]),
+    "fgc_draw_mesh": (_I, [_P, _P, _ST, _SH, _INFO]),
+    "fgc_draw_triangles": (_I, [_P, _P, _U64, _U64, _ST, _SH, _INFO]),
+    "fgc_draw_lines": (_I, [_P, _P, _U64, _U64, _ST, _SH, _INFO]),
+    "fgc_read_color": (_I, [_P, ctypes.POINTER(ctypes.c_uint8)]),
+    "fgc_read_depth": (_I, [_P, _D]),
+    "fgc_write_color": (_I, [_P, ctypes.POINTER(ctypes.c_uint8)]),
+    "fgc_write_depth": (_I, [_P, _D]),
+    "fgc_depth_image": (_I, [_P, ctypes.POINTER(ctypes.c_uint16)]),
+    "fgc_downsample": (_I, [_P, _I32, ctypes.POINTER(ctypes.c_uint8)]),
+    "fgc_read_winner": (_I, [_P, ctypes.POINTER(ctypes.c_uint32)]),
+    "fgc_read_shaded_color": (_I, [_P, _D]),
+}
+
+_lib = None
+
+
+class FauxGLError(RuntimeError):
+    """A libfauxglcuda call returned a non-zero fgc_status."""
+
+    def __init__(self, status, message):
+        super().__init__("fgc status %d: %s" % (status, message))
+        self.status = status
+
+
+def load_library(path=None):
+    """Load libfauxglcuda.so once and bind every exported symbol.
+
+    Raises RuntimeError when the shared library is missing: the CUDA
+    extension is the only implementation of the drawing calls.
+    """
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(
+            "libfauxglcuda.so is not built (%s); run __graft_entry__.build() "
+            "or python -m fauxgl_gb300.build" % p)
+    lib = ctypes.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(status):
+    """Raise FauxGLError for a non-zero fgc_status."""
+    if status != FGC_OK:
+        msg = load_library().fgc_last_error()
+        raise FauxGLError(status, msg.decode() if msg else "")
+    return status
+
+
+def dptr(a):
+    """ctypes double* of a C-contiguous float64 numpy array (or None)."""
+    if a is None:
+        return None
+    return a.ctypes.data_as(_D)

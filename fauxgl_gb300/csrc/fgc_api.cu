@@ -1,0 +1,916 @@
+// fgc_api.cu -- host runtime of libfauxglcuda: the C ABI of
+// include/fauxglcuda.h, context / mesh / texture residency and the draw
+// pipeline orchestration.
+//
+// A draw is one stream-ordered pipeline with a single host synchronisation
+// at its end (RasterizeInfo is returned by value, as DrawMesh returns it,
+// context.go:435-439):
+//   vertex_kernel            per unique position: Output, Outside, NDC, screen
+//   setup_triangles_kernel   culling, edge setup, ordered compaction
+//   setup_lines_kernel       lines after triangles (DrawMesh order)
+//   clip_*_kernel            ClipTriangle / ClipLine for flagged elements
+//   bin_count / scan / bin_scatter   stable band bins
+//   raster_kernel            fragments, shading, ordered resolve
+// Buffers grow on demand; when a kernel reports that a buffer was too small
+// (status word) the raster kernel leaves the framebuffer untouched and the
+// host re-runs the draw with the size the device measured.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+
+#include "fgc_internal.cuh"
+
+using namespace fgc;
+
+namespace {
+
+thread_local std::string g_err = "";
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+#define FGC_CUDA(call)                                                                                        \
+    do {                                                                                                      \
+        cudaError_t e_ = (call);                                                                              \
+        if (e_ != cudaSuccess) return fail(FGC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    // Make room for n elements (contents not preserved when it grows).
+    cudaError_t ensure(size_t n) {
+        if (n <= cap && p) return cudaSuccess;
+        release();
+        size_t want = std::max<size_t>(n + n / 4, 64);
+        cudaError_t e = cudaMalloc((void**)&p, want * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return e;
+        }
+        cap = want;
+        return cudaSuccess;
+    }
+};
+
+struct Counters {
+    unsigned int status;
+    unsigned int clip_count;
+    unsigned int lclip_count;
+    unsigned int band_counter;
+    unsigned int tick_tri, tick_line, tick_scan, pad;
+    unsigned long long tri_slots, line_slots, prim_total, pair_total;
+    unsigned long long info[2];
+};
+
+constexpr int kRasterThreads = 256;
+constexpr int64_t kBandTarget = 4096;  // pixels per band (rounded to whole rows)
+constexpr int kFragCap = 1024;
+constexpr int kMaxBands = 24576;
+
+int grid_for(uint64_t n, int block, int cap) {
+    uint64_t g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > (uint64_t)cap) g = cap;
+    return (int)g;
+}
+
+uint32_t pack_nrgba_host(const double c[4]) {
+    uint32_t out = 0;
+    for (int k = 0; k < 4; k++) {
+        double v = c[k];
+        if (v < 0) v = 0;
+        if (v > 1) v = 1;
+        double s = v * 255.0;
+        uint32_t b = (s == s) ? (uint32_t)(int64_t)s : 0u;  // truncation, NaN -> 0
+        out |= (b & 0xff) << (8 * k);
+    }
+    return out;
+}
+
+}  // namespace
+
+struct fgc_texture {
+    int device = 0;
+    int32_t w = 0, h = 0;
+    DevBuf<ushort4> texels;
+};
+
+struct fgc_mesh {
+    int device = 0;
+    uint64_t ntri = 0, nline = 0, nuniq = 0;
+    DevBuf<double> ux, uy, uz;
+    DevBuf<uint32_t> corner_uniq;
+    DevBuf<APosNrm64> pn64;
+    DevBuf<APosNrm32> pn32;
+    DevBuf<double> tex64, col64;
+    DevBuf<float> tex32, col32;
+    bool has_tex = false, has_col = false;
+
+    MeshView view() const {
+        MeshView v;
+        v.ntri = ntri;
+        v.nline = nline;
+        v.nuniq = nuniq;
+        v.upos_x = ux.p;
+        v.upos_y = uy.p;
+        v.upos_z = uz.p;
+        v.corner_uniq = corner_uniq.p;
+        v.pn64 = pn64.p;
+        v.tex64 = has_tex ? tex64.p : nullptr;
+        v.col64 = has_col ? col64.p : nullptr;
+        v.pn32 = pn32.p;
+        v.tex32 = has_tex ? tex32.p : nullptr;
+        v.col32 = has_col ? col32.p : nullptr;
+        return v;
+    }
+};
+
+struct fgc_context {
+    int device = 0;
+    int sms = 1;
+    cudaStream_t stream = nullptr;
+    int32_t W = 0, H = 0;
+    int64_t N = 0;
+    DevBuf<uint32_t> color;
+    DevBuf<double> depth;
+    bool clear_color_pending = false, clear_depth_pending = false;
+    uint32_t clear_color = 0;
+    double clear_depth = 1.7976931348623157e308;
+    int debug = 0;
+    DevBuf<uint32_t> winner;
+    DevBuf<double> shaded, dbg;
+    // per-draw scratch
+    DevBuf<VClip> vclip;
+    DevBuf<double2> vndc;
+    DevBuf<VScreen> vscr;
+    DevBuf<uint8_t> vout;
+    DevBuf<RPrim> prims;
+    DevBuf<PBox> pbox;
+    DevBuf<ulonglong2> clip_list, lclip_list;
+    DevBuf<PoolVertex> pool;
+    DevBuf<uint32_t> mat, off, bins;
+    DevBuf<unsigned long long> tiles;
+    DevBuf<Counters> counters;
+    DevBuf<unsigned long long> lohi;
+    DevBuf<uint32_t> ds;
+    DevBuf<uint16_t> gray;
+    Counters* host_counters = nullptr;
+    uint32_t clip_cap = 1024;
+    uint64_t bin_cap = 0;
+    std::mutex mu;
+};
+
+namespace {
+
+int apply_pending_clears(fgc_context* c) {
+    int grid = grid_for((uint64_t)c->N, 256, c->sms * 8);
+    if (c->clear_color_pending) {
+        fill_u32_kernel<<<grid, 256, 0, c->stream>>>(c->color.p, (uint64_t)c->N, c->clear_color);
+        FGC_CUDA(cudaGetLastError());
+        c->clear_color_pending = false;
+    }
+    if (c->clear_depth_pending) {
+        fill_f64_kernel<<<grid, 256, 0, c->stream>>>(c->depth.p, (uint64_t)c->N, c->clear_depth);
+        FGC_CUDA(cudaGetLastError());
+        c->clear_depth_pending = false;
+    }
+    return FGC_OK;
+}
+
+int ensure_debug(fgc_context* c) {
+    if (!(c->debug & (FGC_DEBUG_WINNER | FGC_DEBUG_SHADED_COLOR))) return FGC_OK;
+    int grid = grid_for((uint64_t)c->N, 256, c->sms * 8);
+    if ((c->debug & FGC_DEBUG_WINNER) && !c->winner.p) {
+        FGC_CUDA(c->winner.ensure((size_t)c->N));
+        fill_u32_kernel<<<grid, 256, 0, c->stream>>>(c->winner.p, (uint64_t)c->N, 0xFFFFFFFFu);
+        FGC_CUDA(cudaGetLastError());
+    }
+    if ((c->debug & FGC_DEBUG_SHADED_COLOR) && !c->shaded.p) {
+        FGC_CUDA(c->shaded.ensure((size_t)c->N * 4));
+        FGC_CUDA(cudaMemsetAsync(c->shaded.p, 0, (size_t)c->N * 4 * sizeof(double), c->stream));
+    }
+    return FGC_OK;
+}
+
+int fill_views(const fgc_state* st, const fgc_shader* sh, StateView& sv, ShaderView& shv) {
+    if (sh->kind != FGC_SHADER_SOLID_COLOR && sh->kind != FGC_SHADER_TEXTURE && sh->kind != FGC_SHADER_PHONG)
+        return fail(FGC_ERR_UNSUPPORTED_SHADER, "shader kind is not a built-in shader");
+    if (st->cull < FGC_CULL_NONE || st->cull > FGC_CULL_BACK)
+        return fail(FGC_ERR_INVALID_ARGUMENT, "cull must be FGC_CULL_NONE, FGC_CULL_FRONT or FGC_CULL_BACK");
+    if (st->front_face != FGC_FACE_CW && st->front_face != FGC_FACE_CCW)
+        return fail(FGC_ERR_INVALID_ARGUMENT, "front_face must be FGC_FACE_CW or FGC_FACE_CCW");
+    if (st->precision != FGC_PRECISION_PLAIN && st->precision != FGC_PRECISION_MIXED)
+        return fail(FGC_ERR_INVALID_ARGUMENT, "precision must be FGC_PRECISION_PLAIN or FGC_PRECISION_MIXED");
+    if (sh->kind == FGC_SHADER_TEXTURE && !sh->texture)
+        return fail(FGC_ERR_INVALID_ARGUMENT, "TextureShader needs a texture");
+    sv.read_depth = st->read_depth != 0;
+    sv.write_depth = st->write_depth != 0;
+    sv.write_color = st->write_color != 0;
+    sv.alpha_blend = st->alpha_blend != 0;
+    sv.wireframe = st->wireframe != 0;
+    sv.front_face = st->front_face;
+    sv.cull = st->cull;
+    sv.precision = st->precision;
+    sv.line_width = st->line_width;
+    sv.depth_bias = st->depth_bias;
+    memset(&shv, 0, sizeof(shv));
+    shv.kind = sh->kind;
+    memcpy(shv.m, sh->matrix, sizeof(shv.m));
+    memcpy(shv.color, sh->color, sizeof(shv.color));
+    memcpy(shv.light, sh->light_direction, sizeof(shv.light));
+    memcpy(shv.eye, sh->camera_position, sizeof(shv.eye));
+    memcpy(shv.ambient, sh->ambient_color, sizeof(shv.ambient));
+    memcpy(shv.diffuse, sh->diffuse_color, sizeof(shv.diffuse));
+    memcpy(shv.specular, sh->specular_color, sizeof(shv.specular));
+    shv.power = sh->specular_power;
+    shv.object_is_discard = (sh->color[0] == 0 && sh->color[1] == 0 && sh->color[2] == 0 && sh->color[3] == 0);
+    if (sh->texture) {
+        shv.has_texture = 1;
+        shv.tex.texels = sh->texture->texels.p;
+        shv.tex.w = sh->texture->w;
+        shv.tex.h = sh->texture->h;
+    }
+    return FGC_OK;
+}
+
+struct DrawShape {
+    int32_t R;
+    int64_t L;
+    uint32_t nbands;
+    int F;
+    size_t smem;
+    int bin_warps;
+    uint32_t nblk;
+};
+
+int draw_shape(const fgc_context* c, DrawShape& s) {
+    int64_t R = std::max<int64_t>(1, kBandTarget / c->W);
+    R = std::min<int64_t>(R, kRasterThreads - 2);
+    R = std::min<int64_t>(R, c->H);
+    s.R = (int32_t)R;
+    s.L = R * c->W;
+    if (s.L > 65535) return fail(FGC_ERR_UNSUPPORTED, "frame width above 65535 pixels is not supported");
+    s.nbands = (uint32_t)((c->N + s.L - 1) / s.L);
+    if (s.nbands > (uint32_t)kMaxBands) return fail(FGC_ERR_UNSUPPORTED, "frame has too many bands");
+    s.F = kFragCap;
+    s.smem = raster_smem_bytes(s.L, s.F, kRasterThreads);
+    while (s.smem > 227 * 1024 && s.F > 256) {
+        s.F /= 2;
+        s.smem = raster_smem_bytes(s.L, s.F, kRasterThreads);
+    }
+    if (s.smem > 227 * 1024) return fail(FGC_ERR_UNSUPPORTED, "frame too wide for the band rasteriser");
+    int warps = (int)std::min<int64_t>(8, (96 * 1024) / ((int64_t)s.nbands * 4));
+    if (warps < 1) return fail(FGC_ERR_UNSUPPORTED, "frame has too many bands for binning");
+    s.bin_warps = warps;
+    s.nblk = (uint32_t)(2 * c->sms);
+    return FGC_OK;
+}
+
+int run_draw(fgc_context* c, const fgc_mesh* m, uint64_t tf, uint64_t tc, uint64_t lf, uint64_t lc,
+             const StateView& sv, const ShaderView& shv, bool* retry) {
+    *retry = false;
+    DrawShape shape;
+    int rc = draw_shape(c, shape);
+    if (rc) return rc;
+    const int per = sv.wireframe ? 6 : 1;
+    const uint64_t prim_cap = tc * per + (uint64_t)c->clip_cap * (uint64_t)(7 * per - per) + lc * 2 + 1;
+    const uint64_t tri_tiles = (tc + 255) / 256, line_tiles = (lc + 255) / 256;
+    const uint64_t nmat = (uint64_t)shape.nbands * shape.nblk;
+    const uint64_t scan_tiles = (nmat + 2047) / 2048;
+    if (c->bin_cap == 0) c->bin_cap = std::max<uint64_t>(2 * prim_cap, 1 << 16);
+
+    FGC_CUDA(c->vclip.ensure(m->nuniq + 1));
+    FGC_CUDA(c->vndc.ensure(m->nuniq + 1));
+    FGC_CUDA(c->vscr.ensure(m->nuniq + 1));
+    FGC_CUDA(c->vout.ensure(m->nuniq + 1));
+    FGC_CUDA(c->prims.ensure(prim_cap));
+    FGC_CUDA(c->pbox.ensure(prim_cap));
+    FGC_CUDA(c->clip_list.ensure(c->clip_cap));
+    FGC_CUDA(c->pool.ensure((size_t)c->clip_cap * 21));
+    FGC_CUDA(c->lclip_list.ensure(lc + 1));
+    FGC_CUDA(c->mat.ensure(nmat));
+    FGC_CUDA(c->off.ensure(nmat));
+    FGC_CUDA(c->bins.ensure(c->bin_cap));
+    FGC_CUDA(c->tiles.ensure(tri_tiles + line_tiles + scan_tiles + 3));
+    FGC_CUDA(c->counters.ensure(1));
+    if (!c->host_counters) FGC_CUDA(cudaMallocHost((void**)&c->host_counters, sizeof(Counters)));
+    rc = ensure_debug(c);
+    if (rc) return rc;
+
+    FGC_CUDA(cudaMemsetAsync(c->counters.p, 0, sizeof(Counters), c->stream));
+    FGC_CUDA(cudaMemsetAsync(c->tiles.p, 0, (tri_tiles + line_tiles + scan_tiles + 3) * 8, c->stream));
+    Counters* dc = c->counters.p;
+    unsigned long long* t_tri = c->tiles.p;
+    unsigned long long* t_line = t_tri + tri_tiles + 1;
+    unsigned long long* t_scan = t_line + line_tiles + 1;
+
+    const double w2 = (double)c->W / 2, h2 = (double)c->H / 2;
+    if (m->nuniq > 0 && (tc > 0 || lc > 0)) {
+        VertexParams vp;
+        vp.ux = m->ux.p;
+        vp.uy = m->uy.p;
+        vp.uz = m->uz.p;
+        vp.n = m->nuniq;
+        memcpy(vp.m, shv.m, sizeof(vp.m));
+        vp.w2 = w2;
+        vp.h2 = h2;
+        vp.vclip = c->vclip.p;
+        vp.vndc = c->vndc.p;
+        vp.vscr = c->vscr.p;
+        vp.vout = c->vout.p;
+        vertex_kernel<<<grid_for(m->nuniq, 256, c->sms * 16), 256, 0, c->stream>>>(vp);
+        FGC_CUDA(cudaGetLastError());
+    }
+
+    GeomParams gp;
+    memset(&gp, 0, sizeof(gp));
+    gp.mesh = m->view();
+    gp.st = sv;
+    gp.w2 = w2;
+    gp.h2 = h2;
+    gp.tri_first = tf;
+    gp.tri_count = tc;
+    gp.line_first = lf;
+    gp.line_count = lc;
+    gp.vclip = c->vclip.p;
+    gp.vndc = c->vndc.p;
+    gp.vscr = c->vscr.p;
+    gp.vout = c->vout.p;
+    gp.prims = c->prims.p;
+    gp.pbox = c->pbox.p;
+    gp.prim_cap = prim_cap;
+    gp.clip_list = c->clip_list.p;
+    gp.clip_cap = c->clip_cap;
+    gp.clip_count = &dc->clip_count;
+    gp.lclip_list = c->lclip_list.p;
+    gp.lclip_count = &dc->lclip_count;
+    gp.pool = c->pool.p;
+    gp.tri_slots = &dc->tri_slots;
+    gp.line_slots = &dc->line_slots;
+    gp.prim_total = &dc->prim_total;
+    gp.lb_tri = Lookback{t_tri, &dc->tick_tri, &dc->status, &dc->tri_slots};
+    gp.lb_line = Lookback{t_line, &dc->tick_line, &dc->status, &dc->line_slots};
+    gp.status = &dc->status;
+    if (tc > 0) {
+        setup_triangles_kernel<<<(unsigned)tri_tiles, 256, 0, c->stream>>>(gp);
+        FGC_CUDA(cudaGetLastError());
+        clip_triangles_kernel<<<grid_for(c->clip_cap, 128, c->sms * 4), 128, 0, c->stream>>>(gp);
+        FGC_CUDA(cudaGetLastError());
+    }
+    if (lc > 0) {
+        setup_lines_kernel<<<(unsigned)line_tiles, 256, 0, c->stream>>>(gp);
+        FGC_CUDA(cudaGetLastError());
+        clip_lines_kernel<<<grid_for(lc, 128, c->sms * 4), 128, 0, c->stream>>>(gp);
+        FGC_CUDA(cudaGetLastError());
+    }
+    prim_total_kernel<<<1, 1, 0, c->stream>>>(gp);
+    FGC_CUDA(cudaGetLastError());
+
+    BinParams bp;
+    bp.pbox = c->pbox.p;
+    bp.nprim = &dc->prim_total;
+    bp.W = c->W;
+    bp.N = c->N;
+    bp.L = shape.L;
+    bp.nbands = shape.nbands;
+    bp.nblk = shape.nblk;
+    bp.mat = c->mat.p;
+    bp.off = c->off.p;
+    bp.pair_total = &dc->pair_total;
+    bp.bins = c->bins.p;
+    bp.bin_cap = c->bin_cap;
+    bp.status = &dc->status;
+    size_t hist_smem = (size_t)shape.nbands * 4;
+    if (hist_smem > 48 * 1024)
+        FGC_CUDA(cudaFuncSetAttribute(bin_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem));
+    bin_count_kernel<<<shape.nblk, 256, hist_smem, c->stream>>>(bp);
+    FGC_CUDA(cudaGetLastError());
+    ScanParams sp;
+    sp.in = c->mat.p;
+    sp.out = c->off.p;
+    sp.n = nmat;
+    sp.lb = Lookback{t_scan, &dc->tick_scan, &dc->status, &dc->pair_total};
+    scan_u32_kernel<<<(unsigned)scan_tiles, 256, 0, c->stream>>>(sp);
+    FGC_CUDA(cudaGetLastError());
+    size_t scat_smem = (size_t)shape.bin_warps * shape.nbands * 4;
+    if (scat_smem > 48 * 1024)
+        FGC_CUDA(cudaFuncSetAttribute(bin_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scat_smem));
+    bin_scatter_kernel<<<shape.nblk, shape.bin_warps * 32, scat_smem, c->stream>>>(bp, shape.bin_warps);
+    FGC_CUDA(cudaGetLastError());
+
+    RasterParams rp;
+    memset(&rp, 0, sizeof(rp));
+    rp.prims = c->prims.p;
+    rp.pbox = c->pbox.p;
+    rp.bins = c->bins.p;
+    rp.off = c->off.p;
+    rp.pair_total = &dc->pair_total;
+    rp.nblk = shape.nblk;
+    rp.nbands = shape.nbands;
+    rp.W = c->W;
+    rp.H = c->H;
+    rp.N = c->N;
+    rp.L = shape.L;
+    rp.F = shape.F;
+    rp.color = c->color.p;
+    rp.depth = c->depth.p;
+    rp.clear_color_pending = c->clear_color_pending;
+    rp.clear_depth_pending = c->clear_depth_pending;
+    rp.clear_color = c->clear_color;
+    rp.clear_depth = c->clear_depth;
+    rp.st = sv;
+    rp.sh = shv;
+    rp.mesh = m->view();
+    rp.pool = c->pool.p;
+    rp.band_counter = &dc->band_counter;
+    rp.status = &dc->status;
+    rp.info = dc->info;
+    const void* kfn = raster_kernel_ptr(sv.precision);
+    FGC_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shape.smem));
+    int per_sm = 0;
+    FGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kRasterThreads, shape.smem));
+    if (per_sm < 1) return fail(FGC_ERR_UNSUPPORTED, "raster kernel does not fit on an SM");
+    int rgrid = (int)std::min<uint64_t>((uint64_t)per_sm * c->sms, shape.nbands);
+    if (c->debug & FGC_DEBUG_WINNER) rp.winner = c->winner.p;
+    if (c->debug & FGC_DEBUG_SHADED_COLOR) {
+        FGC_CUDA(c->dbg.ensure((size_t)rgrid * shape.F * 4));
+        rp.shaded = c->shaded.p;
+        rp.dbg = c->dbg.p;
+    }
+    FGC_CUDA(launch_raster(sv.precision, rgrid, kRasterThreads, shape.smem, c->stream, rp));
+
+    FGC_CUDA(cudaMemcpyAsync(c->host_counters, c->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream));
+    FGC_CUDA(cudaStreamSynchronize(c->stream));
+    const Counters& hc = *c->host_counters;
+    if (hc.status & ST_LOOKBACK_TIMEOUT)
+        return fail(FGC_ERR_DEVICE_LIMIT, "a look-back wait in the setup or scan stage timed out");
+    if (hc.status & (ST_CLIP_OVERFLOW | ST_POOL_OVERFLOW)) {
+        c->clip_cap = std::max<uint32_t>(c->clip_cap * 2, hc.clip_count + hc.clip_count / 4 + 64);
+        *retry = true;
+        return FGC_OK;
+    }
+    if (hc.status & ST_BIN_OVERFLOW) {
+        c->bin_cap = hc.pair_total + hc.pair_total / 4 + 1024;
+        *retry = true;
+        return FGC_OK;
+    }
+    c->clear_color_pending = false;
+    c->clear_depth_pending = false;
+    return FGC_OK;
+}
+
+int draw(fgc_context* c, const fgc_mesh* m, uint64_t tf, uint64_t tc, uint64_t lf, uint64_t lc,
+         const fgc_state* st, const fgc_shader* sh, fgc_rasterize_info* info) {
+    if (!c || !m || !st || !sh) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
+    if (m->device != c->device) return fail(FGC_ERR_INVALID_ARGUMENT, "mesh and context are on different devices");
+    if (tf > m->ntri || tc > m->ntri - tf) return fail(FGC_ERR_INVALID_ARGUMENT, "triangle range out of bounds");
+    if (lf > m->nline || lc > m->nline - lf) return fail(FGC_ERR_INVALID_ARGUMENT, "line range out of bounds");
+    if (sh->texture && sh->texture->device != c->device)
+        return fail(FGC_ERR_INVALID_ARGUMENT, "texture is on another device");
+    StateView sv;
+    ShaderView shv;
+    int rc = fill_views(st, sh, sv, shv);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lock(c->mu);
+    FGC_CUDA(cudaSetDevice(c->device));
+    for (int attempt = 0; attempt < 8; attempt++) {
+        bool retry = false;
+        rc = run_draw(c, m, tf, tc, lf, lc, sv, shv, &retry);
+        if (rc) return rc;
+        if (!retry) {
+            if (info) {
+                info->total_pixels = c->host_counters->info[0];
+                info->updated_pixels = c->host_counters->info[1];
+            }
+            return FGC_OK;
+        }
+    }
+    return fail(FGC_ERR_DEVICE_LIMIT, "draw buffers kept overflowing");
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int32_t fgc_abi_version(void) { return FGC_ABI_VERSION; }
+
+const char* fgc_last_error(void) { return g_err.c_str(); }
+
+void fgc_state_default(fgc_state* st) {
+    if (!st) return;
+    st->read_depth = 1;
+    st->write_depth = 1;
+    st->write_color = 1;
+    st->alpha_blend = 1;
+    st->wireframe = 0;
+    st->front_face = FGC_FACE_CCW;
+    st->cull = FGC_CULL_BACK;
+    st->precision = FGC_PRECISION_PLAIN;
+    st->line_width = 2;
+    st->depth_bias = 0;
+}
+
+static void shader_common(fgc_shader* sh, int kind, const double matrix[16]) {
+    memset(sh, 0, sizeof(*sh));
+    sh->kind = kind;
+    if (matrix) memcpy(sh->matrix, matrix, sizeof(sh->matrix));
+}
+
+void fgc_shader_solid_color(fgc_shader* sh, const double matrix[16], const double rgba[4]) {
+    if (!sh) return;
+    shader_common(sh, FGC_SHADER_SOLID_COLOR, matrix);
+    if (rgba) memcpy(sh->color, rgba, sizeof(sh->color));
+}
+
+void fgc_shader_texture(fgc_shader* sh, const double matrix[16], const fgc_texture* tex) {
+    if (!sh) return;
+    shader_common(sh, FGC_SHADER_TEXTURE, matrix);
+    sh->texture = tex;
+}
+
+void fgc_shader_phong(fgc_shader* sh, const double matrix[16], const double light_direction[3],
+                      const double camera_position[3]) {
+    if (!sh) return;
+    shader_common(sh, FGC_SHADER_PHONG, matrix);
+    if (light_direction) memcpy(sh->light_direction, light_direction, sizeof(sh->light_direction));
+    if (camera_position) memcpy(sh->camera_position, camera_position, sizeof(sh->camera_position));
+    const double amb[4] = {0.2, 0.2, 0.2, 1}, dif[4] = {0.8, 0.8, 0.8, 1}, spe[4] = {1, 1, 1, 1};
+    memcpy(sh->ambient_color, amb, sizeof(amb));
+    memcpy(sh->diffuse_color, dif, sizeof(dif));
+    memcpy(sh->specular_color, spe, sizeof(spe));
+    sh->specular_power = 32;
+}
+
+int fgc_context_create(int32_t width, int32_t height, fgc_context** out) {
+    if (!out) return fail(FGC_ERR_INVALID_ARGUMENT, "out is null");
+    *out = nullptr;
+    if (width < 1 || height < 1) return fail(FGC_ERR_INVALID_ARGUMENT, "width and height must be positive");
+    if ((int64_t)width * height > (int64_t)1 << 34) return fail(FGC_ERR_INVALID_ARGUMENT, "frame too large");
+    fgc_context* c = new (std::nothrow) fgc_context();
+    if (!c) return fail(FGC_ERR_OUT_OF_MEMORY, "host allocation failed");
+    auto bail = [&](int rc) {
+        delete c;
+        return rc;
+    };
+    cudaError_t e = cudaGetDevice(&c->device);
+    if (e != cudaSuccess) return bail(fail(FGC_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e)));
+    cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return bail(fail(FGC_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)));
+    c->W = width;
+    c->H = height;
+    c->N = (int64_t)width * height;
+    if (c->color.ensure((size_t)c->N) != cudaSuccess || c->depth.ensure((size_t)c->N) != cudaSuccess)
+        return bail(fail(FGC_ERR_OUT_OF_MEMORY, "framebuffer allocation failed"));
+    // NewContext: transparent colour buffer, depth cleared to MaxFloat64
+    // (context.go:64-79); applied lazily by the first kernel that needs it.
+    c->clear_color = 0;
+    c->clear_color_pending = true;
+    c->clear_depth = 1.7976931348623157e308;
+    c->clear_depth_pending = true;
+    *out = c;
+    return FGC_OK;
+}
+
+int fgc_context_destroy(fgc_context* c) {
+    if (!c) return FGC_OK;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    if (c->host_counters) cudaFreeHost(c->host_counters);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return FGC_OK;
+}
+
+int fgc_context_size(const fgc_context* c, int32_t* w, int32_t* h) {
+    if (!c) return fail(FGC_ERR_INVALID_ARGUMENT, "null context");
+    if (w) *w = c->W;
+    if (h) *h = c->H;
+    return FGC_OK;
+}
+
+int fgc_context_set_debug(fgc_context* c, int32_t flags) {
+    if (!c) return fail(FGC_ERR_INVALID_ARGUMENT, "null context");
+    std::lock_guard<std::mutex> lock(c->mu);
+    FGC_CUDA(cudaSetDevice(c->device));
+    c->debug = flags;
+    int rc = ensure_debug(c);
+    if (rc) return rc;
+    FGC_CUDA(cudaStreamSynchronize(c->stream));
+    return FGC_OK;
+}
+
+int fgc_clear_color(fgc_context* c, const double rgba[4]) {
+    if (!c || !rgba) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lock(c->mu);
+    c->clear_color = pack_nrgba_host(rgba);
+    c->clear_color_pending = true;
+    return FGC_OK;
+}
+
+int fgc_clear_depth(fgc_context* c, double value) {
+    if (!c) return fail(FGC_ERR_INVALID_ARGUMENT, "null context");
+    std::lock_guard<std::mutex> lock(c->mu);
+    c->clear_depth = value;
+    c->clear_depth_pending = true;
+    return FGC_OK;
+}
+
+int fgc_mesh_upload(const double* tri_pos, const double* tri_nrm, const double* tri_tex, const double* tri_col,
+                    uint64_t ntri, const double* line_pos, const double* line_nrm, const double* line_tex,
+                    const double* line_col, uint64_t nline, fgc_mesh** out) {
+    if (!out) return fail(FGC_ERR_INVALID_ARGUMENT, "out is null");
+    *out = nullptr;
+    if ((ntri && !tri_pos) || (nline && !line_pos)) return fail(FGC_ERR_INVALID_ARGUMENT, "positions are required");
+    const uint64_t V = 3 * ntri + 2 * nline;
+    if (V >= 0x7FFFFFFFull) return fail(FGC_ERR_UNSUPPORTED, "mesh has too many corners (2^31 limit)");
+    fgc_mesh* m = new (std::nothrow) fgc_mesh();
+    if (!m) return fail(FGC_ERR_OUT_OF_MEMORY, "host allocation failed");
+    int dev = 0;
+    cudaGetDevice(&dev);
+    m->device = dev;
+    m->ntri = ntri;
+    m->nline = nline;
+    int sms = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaStream_t s;
+    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete m;
+        return fail(FGC_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+    }
+    int rc = FGC_OK;
+    DevBuf<double> cp, nrm, tmp;
+    DevBuf<uint32_t> table, slot_of, minc, flag, uid;
+    DevBuf<unsigned long long> tiles;
+    DevBuf<unsigned int> st;
+    unsigned long long* h_tot = nullptr;
+    auto step = [&](cudaError_t err, const char* what) {
+        if (err != cudaSuccess && rc == FGC_OK) rc = fail(FGC_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(err));
+        return rc == FGC_OK;
+    };
+    const int grid = grid_for(V, 256, sms * 16);
+    do {
+        if (V == 0) break;
+        if (!step(cp.ensure(V * 3), "alloc positions")) break;
+        if (ntri && !step(cudaMemcpyAsync(cp.p, tri_pos, ntri * 9 * 8, cudaMemcpyHostToDevice, s), "copy positions")) break;
+        if (nline && !step(cudaMemcpyAsync(cp.p + ntri * 9, line_pos, nline * 6 * 8, cudaMemcpyHostToDevice, s), "copy positions")) break;
+        const bool have_nrm = tri_nrm || line_nrm;
+        if (have_nrm) {
+            if (!step(nrm.ensure(V * 3), "alloc normals")) break;
+            if (!step(cudaMemsetAsync(nrm.p, 0, V * 3 * 8, s), "zero normals")) break;
+            if (tri_nrm && !step(cudaMemcpyAsync(nrm.p, tri_nrm, ntri * 9 * 8, cudaMemcpyHostToDevice, s), "copy normals")) break;
+            if (line_nrm && !step(cudaMemcpyAsync(nrm.p + ntri * 9, line_nrm, nline * 6 * 8, cudaMemcpyHostToDevice, s), "copy normals")) break;
+        }
+        // weld positions
+        uint64_t tsize = 1;
+        while (tsize < 2 * V) tsize <<= 1;
+        if (!step(table.ensure(tsize), "alloc weld table")) break;
+        if (!step(minc.ensure(tsize), "alloc weld table")) break;
+        if (!step(slot_of.ensure(V), "alloc weld") || !step(flag.ensure(V), "alloc weld") || !step(uid.ensure(V), "alloc weld")) break;
+        if (!step(st.ensure(1), "alloc status") || !step(cudaMemsetAsync(st.p, 0, 4, s), "zero status")) break;
+        if (!step(cudaMemsetAsync(table.p, 0xFF, tsize * 4, s), "init table")) break;
+        if (!step(cudaMemsetAsync(minc.p, 0xFF, tsize * 4, s), "init table")) break;
+        weld_insert_kernel<<<grid, 256, 0, s>>>(cp.p, V, table.p, tsize - 1, slot_of.p, minc.p, st.p);
+        weld_flag_kernel<<<grid, 256, 0, s>>>(slot_of.p, minc.p, V, flag.p);
+        const uint64_t scan_tiles = (V + 2047) / 2048;
+        if (!step(tiles.ensure(scan_tiles + 2), "alloc scan") || !step(cudaMemsetAsync(tiles.p, 0, (scan_tiles + 2) * 8, s), "zero scan")) break;
+        ScanParams sp;
+        sp.in = flag.p;
+        sp.out = uid.p;
+        sp.n = V;
+        sp.lb = Lookback{tiles.p + 1, (unsigned int*)(st.p), st.p, tiles.p};
+        // the scan's ticket counter and status share the zeroed status word's
+        // neighbour: use a dedicated zeroed word instead
+        DevBuf<unsigned int> tick;
+        if (!step(tick.ensure(1), "alloc ticket") || !step(cudaMemsetAsync(tick.p, 0, 4, s), "zero ticket")) break;
+        sp.lb.ticket = tick.p;
+        scan_u32_kernel<<<(unsigned)scan_tiles, 256, 0, s>>>(sp);
+        if (!step(cudaGetLastError(), "weld kernels")) break;
+        if (!step(cudaMallocHost((void**)&h_tot, 16), "alloc pinned")) break;
+        if (!step(cudaMemcpyAsync(h_tot, tiles.p, 8, cudaMemcpyDeviceToHost, s), "read unique count")) break;
+        if (!step(cudaMemcpyAsync(h_tot + 1, st.p, 4, cudaMemcpyDeviceToHost, s), "read status")) break;
+        if (!step(cudaStreamSynchronize(s), "weld")) break;
+        if (((unsigned int*)(h_tot + 1))[0] != 0) {
+            rc = fail(FGC_ERR_DEVICE_LIMIT, "mesh weld failed");
+            break;
+        }
+        m->nuniq = h_tot[0];
+        if (!step(m->ux.ensure(m->nuniq + 1), "alloc unique") || !step(m->uy.ensure(m->nuniq + 1), "alloc unique") ||
+            !step(m->uz.ensure(m->nuniq + 1), "alloc unique") || !step(m->corner_uniq.ensure(V), "alloc index"))
+            break;
+        weld_emit_kernel<<<grid, 256, 0, s>>>(cp.p, slot_of.p, minc.p, uid.p, V, m->ux.p, m->uy.p, m->uz.p,
+                                              m->corner_uniq.p);
+        if (!step(m->pn64.ensure(V), "alloc attributes") || !step(m->pn32.ensure(V), "alloc attributes")) break;
+        attrs_kernel<<<grid, 256, 0, s>>>(cp.p, have_nrm ? nrm.p : nullptr, V, m->pn64.p, m->pn32.p);
+        if (!step(cudaGetLastError(), "attribute kernels")) break;
+        if (tri_tex || line_tex) {
+            m->has_tex = true;
+            if (!step(m->tex64.ensure(V * 2), "alloc texcoords") || !step(m->tex32.ensure(V * 2), "alloc texcoords")) break;
+            if (!step(cudaMemsetAsync(m->tex64.p, 0, V * 2 * 8, s), "zero texcoords")) break;
+            if (tri_tex && !step(cudaMemcpyAsync(m->tex64.p, tri_tex, ntri * 6 * 8, cudaMemcpyHostToDevice, s), "copy texcoords")) break;
+            if (line_tex && !step(cudaMemcpyAsync(m->tex64.p + ntri * 6, line_tex, nline * 4 * 8, cudaMemcpyHostToDevice, s), "copy texcoords")) break;
+            f64_to_f32_kernel<<<grid, 256, 0, s>>>(m->tex64.p, V * 2, m->tex32.p);
+        }
+        if (tri_col || line_col) {
+            m->has_col = true;
+            if (!step(m->col64.ensure(V * 4), "alloc colours") || !step(m->col32.ensure(V * 4), "alloc colours")) break;
+            if (!step(cudaMemsetAsync(m->col64.p, 0, V * 4 * 8, s), "zero colours")) break;
+            if (tri_col && !step(cudaMemcpyAsync(m->col64.p, tri_col, ntri * 12 * 8, cudaMemcpyHostToDevice, s), "copy colours")) break;
+            if (line_col && !step(cudaMemcpyAsync(m->col64.p + ntri * 12, line_col, nline * 8 * 8, cudaMemcpyHostToDevice, s), "copy colours")) break;
+            f64_to_f32_kernel<<<grid, 256, 0, s>>>(m->col64.p, V * 4, m->col32.p);
+        }
+        if (!step(cudaGetLastError(), "attribute kernels")) break;
+        step(cudaStreamSynchronize(s), "mesh upload");
+    } while (0);
+    cudaStreamSynchronize(s);
+    if (h_tot) cudaFreeHost(h_tot);
+    cudaStreamDestroy(s);
+    if (rc != FGC_OK) {
+        delete m;
+        return rc;
+    }
+    *out = m;
+    return FGC_OK;
+}
+
+int fgc_mesh_release(fgc_mesh* m) {
+    if (!m) return FGC_OK;
+    cudaSetDevice(m->device);
+    cudaDeviceSynchronize();
+    delete m;
+    return FGC_OK;
+}
+
+int fgc_mesh_counts(const fgc_mesh* m, uint64_t* ntri, uint64_t* nline) {
+    if (!m) return fail(FGC_ERR_INVALID_ARGUMENT, "null mesh");
+    if (ntri) *ntri = m->ntri;
+    if (nline) *nline = m->nline;
+    return FGC_OK;
+}
+
+int fgc_texture_upload(const uint16_t* rgba16, int32_t width, int32_t height, fgc_texture** out) {
+    if (!out || !rgba16) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    if (width < 1 || height < 1) return fail(FGC_ERR_INVALID_ARGUMENT, "texture size must be positive");
+    fgc_texture* t = new (std::nothrow) fgc_texture();
+    if (!t) return fail(FGC_ERR_OUT_OF_MEMORY, "host allocation failed");
+    cudaGetDevice(&t->device);
+    t->w = width;
+    t->h = height;
+    size_t n = (size_t)width * height;
+    cudaError_t e = t->texels.ensure(n);
+    if (e == cudaSuccess) e = cudaMemcpy(t->texels.p, rgba16, n * sizeof(ushort4), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        delete t;
+        return fail(FGC_ERR_CUDA, std::string("texture upload: ") + cudaGetErrorString(e));
+    }
+    *out = t;
+    return FGC_OK;
+}
+
+int fgc_texture_release(fgc_texture* t) {
+    if (!t) return FGC_OK;
+    cudaSetDevice(t->device);
+    cudaDeviceSynchronize();
+    delete t;
+    return FGC_OK;
+}
+
+int fgc_draw_mesh(fgc_context* c, const fgc_mesh* m, const fgc_state* st, const fgc_shader* sh,
+                  fgc_rasterize_info* info) {
+    if (!m) return fail(FGC_ERR_INVALID_ARGUMENT, "null mesh");
+    return draw(c, m, 0, m->ntri, 0, m->nline, st, sh, info);
+}
+
+int fgc_draw_triangles(fgc_context* c, const fgc_mesh* m, uint64_t first, uint64_t count, const fgc_state* st,
+                       const fgc_shader* sh, fgc_rasterize_info* info) {
+    return draw(c, m, first, count, 0, 0, st, sh, info);
+}
+
+int fgc_draw_lines(fgc_context* c, const fgc_mesh* m, uint64_t first, uint64_t count, const fgc_state* st,
+                   const fgc_shader* sh, fgc_rasterize_info* info) {
+    return draw(c, m, 0, 0, first, count, st, sh, info);
+}
+
+int fgc_read_color(fgc_context* c, uint8_t* nrgba) {
+    if (!c || !nrgba) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lock(c->mu);
+    FGC_CUDA(cudaSetDevice(c->device));
+    int rc = apply_pending_clears(c);
+    if (rc) return rc;
+    FGC_CUDA(cudaMemcpyAsync(nrgba, c->color.p, (size_t)c->N * 4, cudaMemcpyDeviceToHost, c->stream));
+    FGC_CUDA(cudaStreamSynchronize(c->stream));
+    return FGC_OK;
+}
+
+int fgc_read_depth(fgc_context* c, double* depth) {
+    if (!c || !depth) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lock(c->mu);
+    FGC_CUDA(cudaSetDevice(c->device));
+    int rc = apply_pending_clears(c);
+    if (rc) return rc;
+    FGC_CUDA(cudaMemcpyAsync(depth, c->depth.p, (size_t)c->N * 8, cudaMemcpyDeviceToHost, c->stream));
+    FGC_CUDA(cudaStreamSynchronize(c->stream));
+    return FGC_OK;
+}
+
+int fgc_write_color(fgc_context* c, const uint8_t* nrgba) {
+    if (!c || !nrgba) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lock(c->mu);
+    FGC_CUDA(cudaSetDevice(c->device));
+    c->clear_color_pending = false;
+    FGC_CUDA(cudaMemcpyAsync(c->color.p, nrgba, (size_t)c->N * 4, cudaMemcpyHostToDevice, c->stream));
+    FGC_CUDA(cudaStreamSynchronize(c->stream));
+    return FGC_OK;
+}
+
+int fgc_write_depth(fgc_context* c, const double* depth) {
+    if (!c || !depth) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lock(c->mu);
+    FGC_CUDA(cudaSetDevice(c->device));
+    c->clear_depth_pending = false;
+    FGC_CUDA(cudaMemcpyAsync(c->depth.p, depth, (size_t)c->N * 8, cudaMemcpyHostToDevice, c->stream));
+    FGC_CUDA(cudaStreamSynchronize(c->stream));
+    return FGC_OK;
+}
+
+int fgc_depth_image(fgc_context* c, uint16_t* gray16) {
+    if (!c || !gray16) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lock(c->mu);
+    FGC_CUDA(cudaSetDevice(c->device));
+    int rc = apply_pending_clears(c);
+    if (rc) return rc;
+    FGC_CUDA(c->lohi.ensure(2));
+    FGC_CUDA(c->gray.ensure((size_t)c->N));
+    unsigned long long init[2] = {~0ull, 0ull};
+    FGC_CUDA(cudaMemcpyAsync(c->lohi.p, init, sizeof(init), cudaMemcpyHostToDevice, c->stream));
+    FGC_CUDA(cudaStreamSynchronize(c->stream));
+    int grid = grid_for((uint64_t)c->N, 256, c->sms * 8);
+    depth_minmax_kernel<<<grid, 256, 0, c->stream>>>(c->depth.p, (uint64_t)c->N, c->lohi.p);
+    depth_image_kernel<<<grid, 256, 0, c->stream>>>(c->depth.p, (uint64_t)c->N, c->lohi.p, c->gray.p);
+    FGC_CUDA(cudaGetLastError());
+    FGC_CUDA(cudaMemcpyAsync(gray16, c->gray.p, (size_t)c->N * 2, cudaMemcpyDeviceToHost, c->stream));
+    FGC_CUDA(cudaStreamSynchronize(c->stream));
+    return FGC_OK;
+}
+
+int fgc_downsample(fgc_context* c, int32_t scale, uint8_t* out) {
+    if (!c || !out) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
+    if (scale < 1 || c->W % scale != 0 || c->H % scale != 0)
+        return fail(FGC_ERR_INVALID_ARGUMENT, "scale must divide width and height");
+    std::lock_guard<std::mutex> lock(c->mu);
+    FGC_CUDA(cudaSetDevice(c->device));
+    int rc = apply_pending_clears(c);
+    if (rc) return rc;
+    const uint64_t n = (uint64_t)(c->W / scale) * (uint64_t)(c->H / scale);
+    FGC_CUDA(c->ds.ensure(n));
+    downsample_kernel<<<grid_for(n, 256, c->sms * 8), 256, 0, c->stream>>>(c->color.p, c->W, c->H, scale, c->ds.p);
+    FGC_CUDA(cudaGetLastError());
+    FGC_CUDA(cudaMemcpyAsync(out, c->ds.p, n * 4, cudaMemcpyDeviceToHost, c->stream));
+    FGC_CUDA(cudaStreamSynchronize(c->stream));
+    return FGC_OK;
+}
+
+int fgc_read_winner(fgc_context* c, uint32_t* winner) {
+    if (!c || !winner) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
+    if (!(c->debug & FGC_DEBUG_WINNER) || !c->winner.p) return fail(FGC_ERR_INVALID_ARGUMENT, "winner ids are off");
+    std::lock_guard<std::mutex> lock(c->mu);
+    FGC_CUDA(cudaSetDevice(c->device));
+    FGC_CUDA(cudaMemcpyAsync(winner, c->winner.p, (size_t)c->N * 4, cudaMemcpyDeviceToHost, c->stream));
+    FGC_CUDA(cudaStreamSynchronize(c->stream));
+    return FGC_OK;
+}
+
+int fgc_read_shaded_color(fgc_context* c, double* rgba) {
+    if (!c || !rgba) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
+    if (!(c->debug & FGC_DEBUG_SHADED_COLOR) || !c->shaded.p)
+        return fail(FGC_ERR_INVALID_ARGUMENT, "shaded colours are off");
+    std::lock_guard<std::mutex> lock(c->mu);
+    FGC_CUDA(cudaSetDevice(c->device));
+    FGC_CUDA(cudaMemcpyAsync(rgba, c->shaded.p, (size_t)c->N * 32, cudaMemcpyDeviceToHost, c->stream));
+    FGC_CUDA(cudaStreamSynchronize(c->stream));
+    return FGC_OK;
+}
+
+}  // extern "C"

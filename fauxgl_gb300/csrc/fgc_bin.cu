@@ -1,0 +1,153 @@
+// fgc_bin.cu -- integer binning of raster primitives into screen bands.
+//
+// A band is a contiguous range of L = R*W linear pixel indices (R whole rows).
+// Binning by linear index rather than by (x, y) reproduces the reference's
+// row wrap-around for free: rasterize only range-checks i = y*W + x against
+// [0, W*H) (context.go:223-228), so a fragment left or right of the screen
+// lands in the neighbouring row, and a primitive whose index range
+// [y0*W + x0, y1*W + x1] meets a band is binned there.
+//
+// The bins must list primitives in submission order (ties resolve "later
+// wins", context.go:248). Count, scan and scatter are all integer and
+// deterministic:
+//   bin_count    per-block band histograms -> mat[band][block]
+//   scan_u32     exclusive scan of mat in (band, block) order -> off
+//   bin_scatter  per block, warps own consecutive sub-ranges; a stable rank
+//                inside each 32-primitive round comes from comparing band
+//                ranges across lanes, so the output order is the input order.
+#include "fgc_internal.cuh"
+
+namespace fgc {
+
+__device__ __forceinline__ bool prim_bands(const BinParams& P, const PBox& b, uint32_t& bl, uint32_t& bh) {
+    if (b.x0 > b.x1) return false;
+    int64_t lo = (int64_t)b.y0 * P.W + b.x0;
+    int64_t hi = (int64_t)b.y1 * P.W + b.x1;
+    if (lo < 0) lo = 0;
+    if (hi > P.N - 1) hi = P.N - 1;
+    if (lo > hi) return false;
+    bl = (uint32_t)(lo / P.L);
+    bh = (uint32_t)(hi / P.L);
+    return true;
+}
+
+constexpr unsigned int kRetryBits = ST_CLIP_OVERFLOW | ST_POOL_OVERFLOW | ST_LOOKBACK_TIMEOUT;
+
+__global__ void __launch_bounds__(256) bin_count_kernel(BinParams P) {
+    extern __shared__ uint32_t hist[];
+    // a failed earlier stage means this draw is re-run: count nothing
+    const uint64_t n = (*P.status & kRetryBits) ? 0 : *P.nprim;
+    const uint64_t chunk = (n + P.nblk - 1) / P.nblk;
+    const uint64_t lo = blockIdx.x * chunk;
+    const uint64_t hi = min(lo + chunk, n);
+    for (uint32_t i = threadIdx.x; i < P.nbands; i += blockDim.x) hist[i] = 0;
+    __syncthreads();
+    for (uint64_t p = lo + threadIdx.x; p < hi; p += blockDim.x) {
+        uint32_t bl, bh;
+        if (prim_bands(P, P.pbox[p], bl, bh))
+            for (uint32_t b = bl; b <= bh; b++) atomicAdd(&hist[b], 1u);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < P.nbands; i += blockDim.x) P.mat[(uint64_t)i * P.nblk + blockIdx.x] = hist[i];
+}
+
+// Exclusive scan of n uint32 values, 2048 per logical block, single pass.
+constexpr int kScanBlock = 256;
+constexpr int kScanItems = 8;
+
+__global__ void __launch_bounds__(kScanBlock) scan_u32_kernel(ScanParams P) {
+    __shared__ uint32_t s_tile;
+    __shared__ OrderedAllocSmem<kScanBlock> s_alloc;
+    const uint32_t tile = block_ticket<kScanBlock>(P.lb, &s_tile);
+    const uint64_t base = ((uint64_t)tile * kScanBlock + threadIdx.x) * kScanItems;
+    uint32_t v[kScanItems];
+    uint64_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        v[k] = (base + k < P.n) ? P.in[base + k] : 0u;
+        sum += v[k];
+    }
+    uint64_t excl = ordered_alloc<kScanBlock>(P.lb, tile, sum, s_alloc);
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        if (base + k < P.n) P.out[base + k] = (uint32_t)excl;
+        excl += v[k];
+    }
+}
+
+__global__ void __launch_bounds__(256) bin_scatter_kernel(BinParams P, int warps) {
+    extern __shared__ uint32_t cnt[];
+    if (*P.pair_total > P.bin_cap) {
+        if (threadIdx.x == 0) atomicOr(P.status, ST_BIN_OVERFLOW);
+        return;
+    }
+    const uint32_t nb = P.nbands;
+    const uint64_t n = (*P.status & kRetryBits) ? 0 : *P.nprim;
+    const uint64_t chunk = (n + P.nblk - 1) / P.nblk;
+    const uint64_t lo = blockIdx.x * chunk;
+    const uint64_t hi = min(lo + chunk, n);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint64_t sub = (chunk + warps - 1) / warps;
+    const uint64_t slo = min(lo + (uint64_t)w * sub, hi);
+    const uint64_t shi = min(slo + sub, hi);
+    uint32_t* mycnt = cnt + (size_t)w * nb;
+
+    for (uint32_t i = threadIdx.x; i < (uint32_t)warps * nb; i += blockDim.x) cnt[i] = 0;
+    __syncthreads();
+    // phase 1: per-warp band counts
+    for (uint64_t p = slo + lane; p < shi; p += 32) {
+        uint32_t bl, bh;
+        if (prim_bands(P, P.pbox[p], bl, bh))
+            for (uint32_t b = bl; b <= bh; b++) atomicAdd(&mycnt[b], 1u);
+    }
+    __syncthreads();
+    // phase 2: each warp's starting position per band
+    for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) {
+        uint32_t run = P.off[(uint64_t)b * P.nblk + blockIdx.x];
+        for (int ww = 0; ww < warps; ww++) {
+            uint32_t t = cnt[(size_t)ww * nb + b];
+            cnt[(size_t)ww * nb + b] = run;
+            run += t;
+        }
+    }
+    __syncthreads();
+    // phase 3: stable scatter, 32 primitives per round in lane order
+    for (uint64_t rb = slo; rb < shi; rb += 32) {
+        const uint64_t p = rb + lane;
+        uint32_t bl = 1, bh = 0;
+        bool has = (p < shi) && prim_bands(P, P.pbox[p], bl, bh);
+        if (!has) { bl = 1; bh = 0; }
+        const uint32_t span = has ? (bh - bl + 1) : 0u;
+        const uint32_t maxspan = __reduce_max_sync(0xffffffffu, span);
+        for (uint32_t k = 0; k < maxspan; k++) {
+            const uint32_t b = bl + k;
+            const bool mine = k < span;
+            uint32_t rank = 0;
+            for (int l2 = 0; l2 < 32; l2++) {
+                uint32_t lo2 = __shfl_sync(0xffffffffu, bl, l2);
+                uint32_t hi2 = __shfl_sync(0xffffffffu, bh, l2);
+                if (mine && l2 < lane && lo2 <= b && b <= hi2) rank++;
+            }
+            if (mine) P.bins[mycnt[b] + rank] = (uint32_t)p;
+        }
+        __syncwarp();
+        for (uint32_t k = 0; k < maxspan; k++) {
+            const uint32_t b = bl + k;
+            const bool mine = k < span;
+            uint32_t rank = 0;
+            bool later = false;
+            for (int l2 = 0; l2 < 32; l2++) {
+                uint32_t lo2 = __shfl_sync(0xffffffffu, bl, l2);
+                uint32_t hi2 = __shfl_sync(0xffffffffu, bh, l2);
+                if (mine && lo2 <= b && b <= hi2) {
+                    if (l2 < lane) rank++;
+                    if (l2 > lane) later = true;
+                }
+            }
+            if (mine && !later) mycnt[b] += rank + 1;
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace fgc

@@ -1,0 +1,432 @@
+// fgc_geometry.cu -- vertex stage, triangle/line setup and view-volume
+// clipping.
+//
+// Pipeline position: mesh (device-resident, positions welded to unique
+// vertices) -> [vertex_kernel] per unique vertex: Output, Outside, NDC,
+// screen position, 1/W -> [setup kernels] per element: culling, screen-space
+// edge setup, ordered compaction of raster primitives (RPrim) -> [clip
+// kernels] for the elements that needed ClipTriangle / ClipLine.
+//
+// Reference: context.go:283-389 (line, wireframe, drawClippedLine,
+// drawClippedTriangle, DrawLine, DrawTriangle), clipping.go (ClipTriangle,
+// ClipLine), vertex.go:14-95, triangle.go:33-58, shader.go:20-23 (Vertex).
+#include "fgc_internal.cuh"
+
+namespace fgc {
+
+// ---------------------------------------------------------------------------
+// Vertex stage: one thread per unique position.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) vertex_kernel(VertexParams P) {
+    for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < P.n; u += (uint64_t)gridDim.x * blockDim.x) {
+        D4 c = mul_position_w(P.m, P.ux[u], P.uy[u], P.uz[u]);  // Shader.Vertex
+        P.vclip[u] = VClip{c.x, c.y, c.z, c.w};
+        P.vout[u] = outside4(c) ? 1 : 0;
+        D3 n = ndc_of(c);
+        P.vndc[u] = make_double2(n.x, n.y);
+        D3 s = screen_of_ndc(n, P.w2, P.h2);
+        P.vscr[u] = VScreen{s.x, s.y, s.z, __ddiv_rn(1.0, c.w)};
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Raster primitive construction: rasterize's per-triangle prologue
+// (context.go:151-181).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double edge_fn(D3 a, D3 b, D3 c) {  // context.go:147-149
+    return __dsub_rn(__dmul_rn(__dsub_rn(b.x, c.x), __dsub_rn(a.y, c.y)),
+                     __dmul_rn(__dsub_rn(b.y, c.y), __dsub_rn(a.x, c.x)));
+}
+
+__device__ void write_dead(const GeomParams& P, uint64_t slot) {
+    if (slot >= P.prim_cap) {
+        atomicOr(P.status, ST_CLIP_OVERFLOW);
+        return;
+    }
+    P.pbox[slot] = PBox{1, 0, 1, 0};
+}
+
+__device__ void make_prim(const GeomParams& P, uint64_t slot, D3 s0, D3 s1, D3 s2, double r0, double r1,
+                          double r2, uint32_t v0, uint32_t v1, uint32_t v2, uint32_t elem) {
+    if (slot >= P.prim_cap) {  // slots reserved past an overflowing clip list
+        atomicOr(P.status, ST_CLIP_OVERFLOW);
+        return;
+    }
+    if (!(dfinite(s0.x) && dfinite(s0.y) && dfinite(s0.z) && dfinite(s1.x) && dfinite(s1.y) && dfinite(s1.z) &&
+          dfinite(s2.x) && dfinite(s2.y) && dfinite(s2.z))) {
+        write_dead(P, slot);
+        return;
+    }
+    // integer bounding box (Min/Max, Floor/Ceil, int())
+    double mnx = floor(go_min(s0.x, go_min(s1.x, s2.x)));
+    double mny = floor(go_min(s0.y, go_min(s1.y, s2.y)));
+    double mxx = ceil(go_max(s0.x, go_max(s1.x, s2.x)));
+    double mxy = ceil(go_max(s0.y, go_max(s1.y, s2.y)));
+    int64_t x0 = go_f2i(mnx), x1 = go_f2i(mxx), y0 = go_f2i(mny), y1 = go_f2i(mxy);
+    const int64_t lim = 1LL << 30;
+    if (x1 - x0 > kMaxExtent || y1 - y0 > kMaxExtent || x0 < -lim || x1 > lim || y0 < -lim || y1 > lim) {
+        write_dead(P, slot);
+        return;
+    }
+    D3 p = d3(__dadd_rn((double)x0, 0.5), __dadd_rn((double)y0, 0.5), 0.0);
+    RPrim R;
+    R.w0 = edge_fn(s1, s2, p);
+    R.w1 = edge_fn(s2, s0, p);
+    R.w2 = edge_fn(s0, s1, p);
+    double a01 = __dsub_rn(s1.y, s0.y);
+    double b01 = __dsub_rn(s0.x, s1.x);
+    double a12 = __dsub_rn(s2.y, s1.y);
+    double b12 = __dsub_rn(s1.x, s2.x);
+    double a20 = __dsub_rn(s0.y, s2.y);
+    double b20 = __dsub_rn(s2.x, s0.x);
+    R.a0 = a12; R.a1 = a20; R.a2 = a01;
+    R.b0 = b12; R.b1 = b20; R.b2 = b01;
+    R.ra = __ddiv_rn(1.0, edge_fn(s0, s1, s2));
+    R.q0 = __ddiv_rn(1.0, a12);
+    R.q1 = __ddiv_rn(1.0, a20);
+    R.q2 = __ddiv_rn(1.0, a01);
+    R.z0 = s0.z; R.z1 = s1.z; R.z2 = s2.z;
+    R.r0 = r0; R.r1 = r1; R.r2 = r2;
+    R.v0 = v0; R.v1 = v1; R.v2 = v2;
+    R.elem = elem;
+    P.prims[slot] = R;
+    P.pbox[slot] = PBox{(int32_t)x0, (int32_t)x1, (int32_t)y0, (int32_t)y1};
+}
+
+// line (context.go:283-294): a screen-space quad of width LineWidth as two
+// raster primitives, (v1,v0,v0; s11,s01,s00) and (v1,v1,v0; s10,s11,s00).
+__device__ void make_line_prims(const GeomParams& P, uint64_t slot, D3 s0, D3 s1, double r0, double r1,
+                                uint32_t v0, uint32_t v1, uint32_t elem) {
+    double lw2 = __ddiv_rn(P.st.line_width, 2.0);
+    D3 d = sub3(s1, s0);
+    D3 perp;  // Perpendicular (vector.go:179-187)
+    if (d.x == 0 && d.y == 0) {
+        perp = (d.z == 0) ? d3(0, 0, 0) : d3(0, 1, 0);
+    } else {
+        perp = normalize3(d3(-d.y, d.x, 0.0));
+    }
+    D3 n = muls3(perp, lw2);
+    s0 = add3(s0, muls3(normalize3(sub3(s0, s1)), lw2));
+    s1 = add3(s1, muls3(normalize3(sub3(s1, s0)), lw2));
+    D3 s00 = add3(s0, n);
+    D3 s01 = sub3(s0, n);
+    D3 s10 = add3(s1, n);
+    D3 s11 = sub3(s1, n);
+    make_prim(P, slot, s11, s01, s00, r1, r0, r0, v1, v0, v0, elem);
+    make_prim(P, slot + 1, s10, s11, s00, r1, r1, r0, v1, v1, v0, elem);
+}
+
+// drawClippedTriangle's cull decision (context.go:322-336) on NDC x/y.
+// Returns +1 to draw in order (v0,v1,v2), -1 to draw swapped (v2,v1,v0),
+// 0 when culled.
+__device__ __forceinline__ int cull_decision(const StateView& st, double n0x, double n0y, double n1x, double n1y,
+                                             double n2x, double n2y) {
+    double a = __dsub_rn(__dmul_rn(__dsub_rn(n1x, n0x), __dsub_rn(n2y, n0y)),
+                         __dmul_rn(__dsub_rn(n2x, n0x), __dsub_rn(n1y, n0y)));
+    int order = (a < 0) ? -1 : 1;
+    if (st.cull == FGC_CULL_FRONT) a = -a;
+    if (st.front_face == FGC_FACE_CW) a = -a;
+    if (st.cull != FGC_CULL_NONE && a <= 0) return 0;
+    return order;
+}
+
+// Emit the primitives of a triangle that survived culling: one, or six for
+// wireframe (context.go:296-301, 344-348).
+__device__ void emit_triangle(const GeomParams& P, uint64_t slot, D3 s0, D3 s1, D3 s2, double r0, double r1,
+                              double r2, uint32_t v0, uint32_t v1, uint32_t v2, uint32_t elem) {
+    if (P.st.wireframe) {
+        make_line_prims(P, slot + 0, s0, s1, r0, r1, v0, v1, elem);
+        make_line_prims(P, slot + 2, s1, s2, r1, r2, v1, v2, elem);
+        make_line_prims(P, slot + 4, s2, s0, r2, r0, v2, v0, elem);
+    } else {
+        make_prim(P, slot, s0, s1, s2, r0, r1, r2, v0, v1, v2, elem);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Triangle setup: one thread per triangle of [first, first+count).
+// ---------------------------------------------------------------------------
+constexpr int kSetupBlock = 256;
+
+__global__ void __launch_bounds__(kSetupBlock) setup_triangles_kernel(GeomParams P) {
+    __shared__ uint32_t s_tile;
+    __shared__ OrderedAllocSmem<kSetupBlock> s_alloc;
+    const uint32_t tile = block_ticket<kSetupBlock>(P.lb_tri, &s_tile);
+    const uint64_t k = (uint64_t)tile * kSetupBlock + threadIdx.x;
+    const bool valid = k < P.tri_count;
+    const uint64_t t = P.tri_first + k;
+    const int per = P.st.wireframe ? 6 : 1;
+
+    uint32_t u0 = 0, u1 = 0, u2 = 0;
+    int order = 0;
+    bool clip = false;
+    if (valid) {
+        u0 = P.mesh.corner_uniq[3 * t + 0];
+        u1 = P.mesh.corner_uniq[3 * t + 1];
+        u2 = P.mesh.corner_uniq[3 * t + 2];
+        clip = (P.vout[u0] | P.vout[u1] | P.vout[u2]) != 0;
+        if (!clip) {
+            double2 n0 = P.vndc[u0], n1 = P.vndc[u1], n2 = P.vndc[u2];
+            order = cull_decision(P.st, n0.x, n0.y, n1.x, n1.y, n2.x, n2.y);
+        }
+    }
+    uint64_t count = !valid ? 0 : (clip ? (uint64_t)(7 * per) : (order != 0 ? (uint64_t)per : 0));
+    uint64_t slot = ordered_alloc<kSetupBlock>(P.lb_tri, tile, count, s_alloc);
+    if (!valid || count == 0) return;
+    if (clip) {
+        uint32_t idx = atomicAdd(P.clip_count, 1u);
+        if (idx < P.clip_cap) {
+            P.clip_list[idx] = make_ulonglong2(t, slot);
+        } else {
+            atomicOr(P.status, ST_CLIP_OVERFLOW);
+        }
+        return;
+    }
+    uint32_t c0 = (uint32_t)(3 * t), c1 = c0 + 1, c2 = c0 + 2;
+    if (order < 0) {  // swap v0 <-> v2
+        uint32_t tu = u0; u0 = u2; u2 = tu;
+        uint32_t tc = c0; c0 = c2; c2 = tc;
+    }
+    VScreen a = P.vscr[u0], b = P.vscr[u1], c = P.vscr[u2];
+    emit_triangle(P, slot, d3(a.x, a.y, a.z), d3(b.x, b.y, b.z), d3(c.x, c.y, c.z), a.rw, b.rw, c.rw, c0, c1, c2,
+                  (uint32_t)t);
+}
+
+// ---------------------------------------------------------------------------
+// Line setup: one thread per line of [first, first+count). Lines always take
+// two slots (dead when clipped away); primitive slots continue after the
+// triangles' (DrawMesh draws lines after triangles, context.go:435-439).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kSetupBlock) setup_lines_kernel(GeomParams P) {
+    __shared__ uint32_t s_tile;
+    __shared__ OrderedAllocSmem<kSetupBlock> s_alloc;
+    const uint32_t tile = block_ticket<kSetupBlock>(P.lb_line, &s_tile);
+    const uint64_t k = (uint64_t)tile * kSetupBlock + threadIdx.x;
+    const bool valid = k < P.line_count;
+    const uint64_t l = P.line_first + k;
+    uint64_t count = valid ? 2 : 0;
+    uint64_t slot = ordered_alloc<kSetupBlock>(P.lb_line, tile, count, s_alloc);
+    if (!valid) return;
+    slot += *P.tri_slots;
+    const uint64_t cb = 3 * P.mesh.ntri + 2 * l;
+    uint32_t u0 = P.mesh.corner_uniq[cb], u1 = P.mesh.corner_uniq[cb + 1];
+    if ((P.vout[u0] | P.vout[u1]) != 0) {
+        uint32_t idx = atomicAdd(P.lclip_count, 1u);
+        P.lclip_list[idx] = make_ulonglong2(l, slot);  // lclip_list holds line_count entries
+        return;
+    }
+    VScreen a = P.vscr[u0], b = P.vscr[u1];
+    make_line_prims(P, slot, d3(a.x, a.y, a.z), d3(b.x, b.y, b.z), a.rw, b.rw, (uint32_t)cb, (uint32_t)(cb + 1),
+                    kLineFlag | (uint32_t)l);
+}
+
+// ---------------------------------------------------------------------------
+// Clipping (clipping.go)
+// ---------------------------------------------------------------------------
+
+// clipPlanes (clipping.go:3-10): {P, N} of +x, -x, +y, -y, +z, -z.
+__device__ __forceinline__ void clip_plane(int k, D4& p, D4& n) {
+    double s = (k & 1) ? -1.0 : 1.0;
+    int axis = k >> 1;
+    p = d4(axis == 0 ? s : 0.0, axis == 1 ? s : 0.0, axis == 2 ? s : 0.0, 1.0);
+    n = d4(axis == 0 ? -s : 0.0, axis == 1 ? -s : 0.0, axis == 2 ? -s : 0.0, 1.0);
+}
+
+__device__ __forceinline__ bool point_in_front(int k, D4 v) {  // clipping.go:16-18
+    D4 p, n;
+    clip_plane(k, p, n);
+    return dot4(sub4(v, p), n) > 0;
+}
+
+__device__ __forceinline__ D4 intersect_segment(int k, D4 v0, D4 v1) {  // clipping.go:20-26
+    D4 p, n;
+    clip_plane(k, p, n);
+    D4 u = sub4(v1, v0);
+    D4 w = sub4(v0, p);
+    double d = dot4(n, u);
+    double nn = -dot4(n, w);
+    return add4(v0, muls4(u, __ddiv_rn(nn, d)));
+}
+
+// Barycentric (vertex.go:81-95).
+__device__ D4 barycentric(D3 p1, D3 p2, D3 p3, D3 p) {
+    D3 v0 = sub3(p2, p1), v1 = sub3(p3, p1), v2 = sub3(p, p1);
+    double d00 = dot3(v0, v0), d01 = dot3(v0, v1), d11 = dot3(v1, v1);
+    double d20 = dot3(v2, v0), d21 = dot3(v2, v1);
+    double d = __dsub_rn(__dmul_rn(d00, d11), __dmul_rn(d01, d01));
+    double v = __ddiv_rn(__dsub_rn(__dmul_rn(d11, d20), __dmul_rn(d01, d21)), d);
+    double w = __ddiv_rn(__dsub_rn(__dmul_rn(d00, d21), __dmul_rn(d01, d20)), d);
+    double u = __dsub_rn(__dsub_rn(1.0, v), w);
+    return d4(u, v, w, 1.0);
+}
+
+struct FullVertex {
+    D3 pos, nrm;
+    double tu, tv, tz;
+    D4 col;
+    D4 out;
+};
+
+// ((0 + a*bX) + b*bY + c*bZ) * bW for one component (vertex.go:49-79).
+__device__ __forceinline__ double interp1(double a, double b, double c, D4 w) {
+    double n = __dadd_rn(0.0, __dmul_rn(a, w.x));
+    n = __dadd_rn(n, __dmul_rn(b, w.y));
+    n = __dadd_rn(n, __dmul_rn(c, w.z));
+    return __dmul_rn(n, w.w);
+}
+
+// InterpolateVertexes (vertex.go:18-47).
+__device__ FullVertex interp_full(const FullVertex& a, const FullVertex& b, const FullVertex& c, D4 w) {
+    FullVertex v;
+    v.pos = d3(interp1(a.pos.x, b.pos.x, c.pos.x, w), interp1(a.pos.y, b.pos.y, c.pos.y, w),
+               interp1(a.pos.z, b.pos.z, c.pos.z, w));
+    v.nrm = normalize3(d3(interp1(a.nrm.x, b.nrm.x, c.nrm.x, w), interp1(a.nrm.y, b.nrm.y, c.nrm.y, w),
+                          interp1(a.nrm.z, b.nrm.z, c.nrm.z, w)));
+    v.tu = interp1(a.tu, b.tu, c.tu, w);
+    v.tv = interp1(a.tv, b.tv, c.tv, w);
+    v.tz = interp1(a.tz, b.tz, c.tz, w);
+    v.col = d4(interp1(a.col.x, b.col.x, c.col.x, w), interp1(a.col.y, b.col.y, c.col.y, w),
+               interp1(a.col.z, b.col.z, c.col.z, w), interp1(a.col.w, b.col.w, c.col.w, w));
+    v.out = d4(interp1(a.out.x, b.out.x, c.out.x, w), interp1(a.out.y, b.out.y, c.out.y, w),
+               interp1(a.out.z, b.out.z, c.out.z, w), interp1(a.out.w, b.out.w, c.out.w, w));
+    return v;
+}
+
+// FixNormals (triangle.go:46-58).
+__device__ void fix_normals(FullVertex& a, FullVertex& b, FullVertex& c) {
+    D3 n = normalize3(cross3(sub3(b.pos, a.pos), sub3(c.pos, a.pos)));
+    if (a.nrm.x == 0 && a.nrm.y == 0 && a.nrm.z == 0) a.nrm = n;
+    if (b.nrm.x == 0 && b.nrm.y == 0 && b.nrm.z == 0) b.nrm = n;
+    if (c.nrm.x == 0 && c.nrm.y == 0 && c.nrm.z == 0) c.nrm = n;
+}
+
+__device__ FullVertex load_corner(const GeomParams& P, uint64_t corner) {
+    FullVertex v;
+    APosNrm64 pn = P.mesh.pn64[corner];
+    v.pos = d3(pn.px, pn.py, pn.pz);
+    v.nrm = d3(pn.nx, pn.ny, pn.nz);
+    v.tu = P.mesh.tex64 ? P.mesh.tex64[2 * corner] : 0.0;
+    v.tv = P.mesh.tex64 ? P.mesh.tex64[2 * corner + 1] : 0.0;
+    v.tz = 0.0;
+    if (P.mesh.col64) {
+        v.col = d4(P.mesh.col64[4 * corner], P.mesh.col64[4 * corner + 1], P.mesh.col64[4 * corner + 2],
+                   P.mesh.col64[4 * corner + 3]);
+    } else {
+        v.col = d4(0, 0, 0, 0);
+    }
+    VClip o = P.vclip[P.mesh.corner_uniq[corner]];
+    v.out = d4(o.x, o.y, o.z, o.w);
+    return v;
+}
+
+// ClipTriangle (clipping.go:54-74) + drawClippedTriangle for each piece.
+// Entry e owns primitive slots [base, base + 7*per) and pool vertices
+// [21e, 21e + 21).
+__global__ void __launch_bounds__(128) clip_triangles_kernel(GeomParams P) {
+    uint32_t n = min(*P.clip_count, P.clip_cap);
+    const int per = P.st.wireframe ? 6 : 1;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        ulonglong2 ent = P.clip_list[e];
+        uint64_t t = ent.x, base = ent.y;
+        FullVertex tv[3];
+        for (int c = 0; c < 3; c++) tv[c] = load_corner(P, 3 * t + c);
+        fix_normals(tv[0], tv[1], tv[2]);  // NewTriangle(v1, v2, v3)
+        D3 p1 = d3(tv[0].out.x, tv[0].out.y, tv[0].out.z);
+        D3 p2 = d3(tv[1].out.x, tv[1].out.y, tv[1].out.z);
+        D3 p3 = d3(tv[2].out.x, tv[2].out.y, tv[2].out.z);
+        // sutherlandHodgman (clipping.go:28-52)
+        D4 bufa[10], bufb[10];
+        bufa[0] = tv[0].out; bufa[1] = tv[1].out; bufa[2] = tv[2].out;
+        int nin = 3;
+        D4* in = bufa;
+        D4* out = bufb;
+        for (int k = 0; k < 6 && nin > 0; k++) {
+            int no = 0;
+            D4 s = in[nin - 1];
+            for (int j = 0; j < nin; j++) {
+                D4 ev = in[j];
+                if (point_in_front(k, ev)) {
+                    if (!point_in_front(k, s)) out[no++] = intersect_segment(k, s, ev);
+                    out[no++] = ev;
+                } else if (point_in_front(k, s)) {
+                    out[no++] = intersect_segment(k, s, ev);
+                }
+                s = ev;
+            }
+            D4* tmp = in; in = out; out = tmp;
+            nin = no;
+        }
+        int sub = 0;
+        for (int i = 2; i < nin && sub < 7; i++, sub++) {
+            D4 bw[3];
+            bw[0] = barycentric(p1, p2, p3, d3(in[0].x, in[0].y, in[0].z));
+            bw[1] = barycentric(p1, p2, p3, d3(in[i - 1].x, in[i - 1].y, in[i - 1].z));
+            bw[2] = barycentric(p1, p2, p3, d3(in[i].x, in[i].y, in[i].z));
+            FullVertex v[3];
+            for (int c = 0; c < 3; c++) v[c] = interp_full(tv[0], tv[1], tv[2], bw[c]);
+            fix_normals(v[0], v[1], v[2]);  // NewTriangle
+            uint32_t pref[3];
+            for (int c = 0; c < 3; c++) {
+                uint32_t pi = e * 21 + sub * 3 + c;
+                P.pool[pi] = PoolVertex{v[c].pos.x, v[c].pos.y, v[c].pos.z, v[c].nrm.x, v[c].nrm.y, v[c].nrm.z,
+                                        v[c].tu, v[c].tv, v[c].col.x, v[c].col.y, v[c].col.z, v[c].col.w};
+                pref[c] = kPoolFlag | pi;
+            }
+            // drawClippedTriangle (context.go:316-349)
+            D3 n0 = ndc_of(v[0].out), n1 = ndc_of(v[1].out), n2 = ndc_of(v[2].out);
+            int order = cull_decision(P.st, n0.x, n0.y, n1.x, n1.y, n2.x, n2.y);
+            uint64_t slot = base + (uint64_t)sub * per;
+            if (order == 0) {
+                for (int q = 0; q < per; q++) write_dead(P, slot + q);
+                continue;
+            }
+            int i0 = 0, i2 = 2;
+            if (order < 0) { i0 = 2; i2 = 0; }
+            D3 nn[3] = {n0, n1, n2};
+            D3 s0 = screen_of_ndc(nn[i0], P.w2, P.h2);
+            D3 s1 = screen_of_ndc(nn[1], P.w2, P.h2);
+            D3 s2 = screen_of_ndc(nn[i2], P.w2, P.h2);
+            emit_triangle(P, slot, s0, s1, s2, __ddiv_rn(1.0, v[i0].out.w), __ddiv_rn(1.0, v[1].out.w),
+                          __ddiv_rn(1.0, v[i2].out.w), pref[i0], pref[1], pref[i2], (uint32_t)t);
+        }
+        for (; sub < 7; sub++)
+            for (int q = 0; q < per; q++) write_dead(P, base + (uint64_t)sub * per + q);
+    }
+}
+
+// ClipLine (clipping.go:76-98) + drawClippedLine (context.go:303-314): only
+// Output moves, the attributes stay the line's own.
+__global__ void __launch_bounds__(128) clip_lines_kernel(GeomParams P) {
+    uint32_t n = *P.lclip_count;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        ulonglong2 ent = P.lclip_list[e];
+        uint64_t l = ent.x, slot = ent.y;
+        uint64_t cb = 3 * P.mesh.ntri + 2 * l;
+        VClip a = P.vclip[P.mesh.corner_uniq[cb]], b = P.vclip[P.mesh.corner_uniq[cb + 1]];
+        D4 w1 = d4(a.x, a.y, a.z, a.w), w2 = d4(b.x, b.y, b.z, b.w);
+        bool culled = false;
+        for (int k = 0; k < 6; k++) {
+            bool f1 = point_in_front(k, w1), f2 = point_in_front(k, w2);
+            if (f1 && f2) continue;
+            else if (f1) w2 = intersect_segment(k, w1, w2);
+            else if (f2) w1 = intersect_segment(k, w2, w1);
+            else { culled = true; break; }
+        }
+        if (culled) {
+            write_dead(P, slot);
+            write_dead(P, slot + 1);
+            continue;
+        }
+        D3 s0 = screen_of_ndc(ndc_of(w1), P.w2, P.h2);
+        D3 s1 = screen_of_ndc(ndc_of(w2), P.w2, P.h2);
+        make_line_prims(P, slot, s0, s1, __ddiv_rn(1.0, w1.w), __ddiv_rn(1.0, w2.w), (uint32_t)cb,
+                        (uint32_t)(cb + 1), kLineFlag | (uint32_t)l);
+    }
+}
+
+// Total primitive slots of the draw (triangles' then lines').
+__global__ void prim_total_kernel(GeomParams P) {
+    *P.prim_total = *P.tri_slots + *P.line_slots;
+}
+
+}  // namespace fgc

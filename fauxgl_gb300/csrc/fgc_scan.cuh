@@ -1,0 +1,124 @@
+// fgc_scan.cuh -- block-wide scans and a single-pass, order-preserving global
+// allocation (decoupled look-back, Merrill & Garland 2016).
+//
+// A kernel that emits a variable number of records per input element calls
+// ordered_alloc(): every thread gets the exclusive prefix of all counts of
+// earlier elements, so records land in submission order with one pass over
+// the input. Logical block indices come from an atomic ticket so every
+// predecessor of a block has already started; each wait on a predecessor is
+// bounded (kSpinLimit polls) and reports ST_LOOKBACK_TIMEOUT instead of
+// hanging.
+#pragma once
+
+#include "fgc_device.cuh"
+
+namespace fgc {
+
+constexpr uint64_t kFlagAgg = 1ull << 62;
+constexpr uint64_t kFlagPre = 2ull << 62;
+constexpr uint64_t kValMask = (1ull << 62) - 1;
+
+struct Lookback {
+    unsigned long long* tiles;  // one word per logical block, zeroed before launch
+    unsigned int* ticket;       // zeroed before launch
+    unsigned int* status;       // device status word
+    unsigned long long* total;  // receives the grand total (written by the last block)
+};
+
+template <int BLOCK>
+__device__ __forceinline__ uint32_t block_ticket(const Lookback& L, uint32_t* s_tile) {
+    if (threadIdx.x == 0) *s_tile = atomicAdd(L.ticket, 1u);
+    __syncthreads();
+    return *s_tile;
+}
+
+// Inclusive warp scan of a 64-bit value.
+__device__ __forceinline__ uint64_t warp_inclusive_scan(uint64_t v) {
+    const unsigned lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint64_t t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= (unsigned)o) v += t;
+    }
+    return v;
+}
+
+// Block exclusive scan; returns the thread's exclusive prefix and writes the
+// block aggregate to *agg. s_warp must hold BLOCK/32 + 1 words.
+template <int BLOCK>
+__device__ __forceinline__ uint64_t block_exclusive_scan(uint64_t v, uint64_t* s_warp, uint64_t* agg) {
+    constexpr int NW = BLOCK / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint64_t inc = warp_inclusive_scan(v);
+    if (lane == 31) s_warp[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        uint64_t w = (lane < NW) ? s_warp[lane] : 0;
+        uint64_t wi = warp_inclusive_scan(w);
+        if (lane < NW) s_warp[lane] = wi - w;
+        if (lane == NW - 1) s_warp[NW] = wi;
+    }
+    __syncthreads();
+    uint64_t r = s_warp[warp] + inc - v;
+    *agg = s_warp[NW];
+    __syncthreads();
+    return r;
+}
+
+// Publish this block's aggregate, look back over predecessors and return the
+// block's exclusive prefix (thread 0 computes; all threads receive it).
+template <int BLOCK>
+__device__ __forceinline__ uint64_t lookback_prefix(const Lookback& L, uint32_t tile, uint64_t agg,
+                                                    uint64_t* s_prefix) {
+    if (threadIdx.x == 0) {
+        uint64_t excl = 0;
+        if (tile == 0) {
+            atomicExch(&L.tiles[0], (unsigned long long)(kFlagPre | (agg & kValMask)));
+        } else {
+            atomicExch(&L.tiles[tile], (unsigned long long)(kFlagAgg | (agg & kValMask)));
+            int64_t j = (int64_t)tile - 1;
+            uint32_t spins = 0;
+            while (j >= 0) {
+                uint64_t s = *(volatile unsigned long long*)&L.tiles[j];
+                uint64_t flag = s & ~kValMask;
+                if (flag == 0) {
+                    if (++spins > kSpinLimit) {
+                        atomicOr(L.status, ST_LOOKBACK_TIMEOUT);
+                        break;
+                    }
+                    __nanosleep(32);
+                    continue;
+                }
+                excl += s & kValMask;
+                if (flag == kFlagPre) break;
+                j--;
+            }
+            atomicExch(&L.tiles[tile], (unsigned long long)(kFlagPre | ((excl + agg) & kValMask)));
+        }
+        if (tile == gridDim.x - 1 && L.total) *L.total = excl + agg;
+        *s_prefix = excl;
+    }
+    __syncthreads();
+    uint64_t r = *s_prefix;
+    __syncthreads();
+    return r;
+}
+
+// One call per thread per launch: exclusive global offset of this thread's
+// count in (logical block, thread) order.
+template <int BLOCK>
+struct OrderedAllocSmem {
+    uint64_t warp[BLOCK / 32 + 1];
+    uint64_t prefix;
+};
+
+template <int BLOCK>
+__device__ __forceinline__ uint64_t ordered_alloc(const Lookback& L, uint32_t tile, uint64_t count,
+                                                  OrderedAllocSmem<BLOCK>& sm) {
+    uint64_t agg;
+    uint64_t local = block_exclusive_scan<BLOCK>(count, sm.warp, &agg);
+    uint64_t base = lookback_prefix<BLOCK>(L, tile, agg, &sm.prefix);
+    return base + local;
+}
+
+}  // namespace fgc

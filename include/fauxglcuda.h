@@ -1,0 +1,210 @@
+/*
+ * fauxglcuda.h -- C ABI of libfauxglcuda, the GB300 (sm_103a) implementation of
+ * FauxGL's triangle pipeline.
+ *
+ * The ABI is what a cgo wrapper of package fauxgl binds:
+ * plain C types, opaque handles, host arrays borrowed only for the duration of
+ * a call. Every function returns an fgc_status (0 = FGC_OK). A failing call
+ * leaves a message retrievable with fgc_last_error().
+ *
+ * Reference interfaces replaced (file:line in fogleman/fauxgl):
+ *   fgc_context_create      NewContext                     context.go:60-81
+ *   fgc_clear_color         Context.ClearColorBufferWith   context.go:119-131
+ *                           (ClearColorBuffer = ...With(dc.ClearColor), context.go:133-135)
+ *   fgc_clear_depth         Context.ClearDepthBufferWith   context.go:137-141
+ *                           (ClearDepthBuffer = ...With(math.MaxFloat64), context.go:143-145)
+ *   fgc_mesh_upload         Mesh{Triangles, Lines}         mesh.go:9-13 (+ Triangle/Line/Vertex,
+ *                                                          triangle.go:3-5, line.go:3-5, vertex.go:3-12)
+ *   fgc_texture_upload      ImageTexture                   texture.go:21-31
+ *   fgc_draw_mesh           Context.DrawMesh               context.go:435-439
+ *   fgc_draw_triangles      Context.DrawTriangles          context.go:413-433
+ *                           (DrawTriangle = a draw of one triangle, context.go:370-389)
+ *   fgc_draw_lines          Context.DrawLines              context.go:391-411
+ *                           (DrawLine = a draw of one line, context.go:351-368)
+ *   fgc_read_color          Context.Image / ColorBuffer    context.go:83-85, 43
+ *   fgc_read_depth          Context.DepthBuffer            context.go:44
+ *   fgc_write_color/_depth  host writes into ColorBuffer / DepthBuffer (public fields)
+ *   fgc_depth_image         Context.DepthImage             context.go:87-117
+ *   fgc_downsample          (no reference counterpart: the examples call the third-party
+ *                           resize.Resize after Image(), README.md:107-109)
+ *
+ * Draw state (fgc_state) mirrors the public Context fields (context.go:40-58);
+ * shader parameters (fgc_shader) mirror SolidColorShader / TextureShader /
+ * PhongShader (shader.go:10-59). A Go Shader that is not one of the three
+ * built-ins cannot be expressed here: the wrapper rejects it with an error,
+ * there is no CPU fallback.
+ */
+#ifndef FAUXGLCUDA_H
+#define FAUXGLCUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FGC_ABI_VERSION 1
+
+typedef enum fgc_status {
+    FGC_OK = 0,
+    FGC_ERR_INVALID_ARGUMENT = 1,   /* bad handle, size or enum value              */
+    FGC_ERR_UNSUPPORTED_SHADER = 2, /* shader kind is not a built-in               */
+    FGC_ERR_CUDA = 3,               /* a CUDA runtime call failed                  */
+    FGC_ERR_OUT_OF_MEMORY = 4,      /* device allocation failed                    */
+    FGC_ERR_DEVICE_LIMIT = 5,       /* a kernel hit a bounded limit and gave up     */
+    FGC_ERR_UNSUPPORTED = 6         /* valid request outside what this build does  */
+} fgc_status;
+
+/* Face and Cull take the reference's enum values (context.go:11-26). */
+enum { FGC_FACE_CW = 1, FGC_FACE_CCW = 2 };
+enum { FGC_CULL_NONE = 1, FGC_CULL_FRONT = 2, FGC_CULL_BACK = 3 };
+
+/* Built-in shader kinds (shader.go). */
+enum { FGC_SHADER_SOLID_COLOR = 1, FGC_SHADER_TEXTURE = 2, FGC_SHADER_PHONG = 3 };
+
+/* Arithmetic forms. PLAIN computes every stage in FP64 in the reference's
+ * operation order. MIXED keeps FP64 for the vertex transform, triangle setup,
+ * edge functions and depth, and runs interpolation and shading in FP32. */
+enum { FGC_PRECISION_PLAIN = 0, FGC_PRECISION_MIXED = 1 };
+
+/* Debug outputs a context may keep beside its framebuffer (fgc_context_set_debug). */
+enum { FGC_DEBUG_WINNER = 1, FGC_DEBUG_SHADED_COLOR = 2 };
+
+typedef struct fgc_context fgc_context;
+typedef struct fgc_mesh fgc_mesh;
+typedef struct fgc_texture fgc_texture;
+
+/* RasterizeInfo (context.go:28-31). */
+typedef struct fgc_rasterize_info {
+    uint64_t total_pixels;
+    uint64_t updated_pixels;
+} fgc_rasterize_info;
+
+/* Per-draw snapshot of the public Context fields (context.go:40-58). Booleans
+ * are 0/1. NewContext's defaults (context.go:66-77) are what
+ * fgc_state_default() writes. */
+typedef struct fgc_state {
+    int32_t read_depth;
+    int32_t write_depth;
+    int32_t write_color;
+    int32_t alpha_blend;
+    int32_t wireframe;
+    int32_t front_face;   /* FGC_FACE_*                    */
+    int32_t cull;         /* FGC_CULL_*                    */
+    int32_t precision;    /* FGC_PRECISION_* (new knob)    */
+    double line_width;
+    double depth_bias;
+} fgc_state;
+
+/* Built-in shader parameters (shader.go:10-59). matrix is row-major
+ * (Matrix.X00, X01, ... X33, matrix.go:5-10). color is SolidColorShader.Color
+ * or PhongShader.ObjectColor. texture is TextureShader.Texture or
+ * PhongShader.Texture (NULL = none). */
+typedef struct fgc_shader {
+    int32_t kind;         /* FGC_SHADER_* */
+    int32_t reserved;
+    double matrix[16];
+    double color[4];
+    double light_direction[3];
+    double camera_position[3];
+    double ambient_color[4];
+    double diffuse_color[4];
+    double specular_color[4];
+    double specular_power;
+    const fgc_texture* texture;
+} fgc_shader;
+
+/* ---- library ------------------------------------------------------------ */
+int32_t fgc_abi_version(void);
+/* Fill *st with NewContext's defaults (context.go:66-77): ReadDepth, WriteDepth,
+ * WriteColor, AlphaBlend on; Wireframe off; FaceCCW; CullBack; LineWidth 2;
+ * DepthBias 0; precision PLAIN. */
+void fgc_state_default(fgc_state* st);
+/* NewSolidColorShader / NewTextureShader / NewPhongShader (shader.go:14-16, 33-35, 61-68). */
+void fgc_shader_solid_color(fgc_shader* sh, const double matrix[16], const double rgba[4]);
+void fgc_shader_texture(fgc_shader* sh, const double matrix[16], const fgc_texture* tex);
+void fgc_shader_phong(fgc_shader* sh, const double matrix[16], const double light_direction[3],
+                      const double camera_position[3]);
+/* Message of the last failed call on this thread (never NULL). */
+const char* fgc_last_error(void);
+
+/* ---- context ------------------------------------------------------------ */
+/* NewContext(width, height): device-resident NRGBA colour (4 B/px) and FP64
+ * depth (8 B/px) buffers. The colour buffer starts transparent (all zero) and
+ * the depth buffer at math.MaxFloat64, as in the reference. Uses the current
+ * CUDA device; every call on the context runs on the context's own stream. */
+int fgc_context_create(int32_t width, int32_t height, fgc_context** out);
+int fgc_context_destroy(fgc_context* ctx);
+int fgc_context_size(const fgc_context* ctx, int32_t* width, int32_t* height);
+/* Keep winner ids (element index of the last fragment that updated each pixel,
+ * lines with bit 31 set, 0xFFFFFFFF where none) and/or the FP64 shader output
+ * of that fragment, for parity tests. 0 turns both off. */
+int fgc_context_set_debug(fgc_context* ctx, int32_t flags);
+
+/* ClearColorBufferWith(c): every pixel becomes c.NRGBA() (color.go:56-63). */
+int fgc_clear_color(fgc_context* ctx, const double rgba[4]);
+/* ClearDepthBufferWith(v). */
+int fgc_clear_depth(fgc_context* ctx, double value);
+
+/* ---- resources ---------------------------------------------------------- */
+/* Upload a triangle soup plus a line list as a device-resident mesh.
+ *   tri_pos  ntri*9   V1.Position xyz, V2.Position xyz, V3.Position xyz
+ *   tri_nrm  ntri*9   normals, same layout, or NULL (all zero)
+ *   tri_tex  ntri*6   Vertex.Texture X,Y per corner, or NULL (Texture.Z never
+ *                     reaches an output and is not stored)
+ *   tri_col  ntri*12  Vertex.Color RGBA per corner, or NULL
+ *   line_*   the same per line with 2 corners (6, 6, 4, 8 values per line).
+ * Host arrays are read during the call only. The mesh lives on the current
+ * device and may be drawn by any context on that device. */
+int fgc_mesh_upload(const double* tri_pos, const double* tri_nrm, const double* tri_tex,
+                    const double* tri_col, uint64_t ntri,
+                    const double* line_pos, const double* line_nrm, const double* line_tex,
+                    const double* line_col, uint64_t nline, fgc_mesh** out);
+int fgc_mesh_release(fgc_mesh* mesh);
+int fgc_mesh_counts(const fgc_mesh* mesh, uint64_t* ntri, uint64_t* nline);
+
+/* ImageTexture: texels as the 16-bit alpha-premultiplied RGBA that
+ * image.Image.At(x, y).RGBA() returns, row-major, width*height*4 values.
+ * BilinearSample (texture.go:41-63) converts them with MakeColor (color.go:25-29). */
+int fgc_texture_upload(const uint16_t* rgba16, int32_t width, int32_t height, fgc_texture** out);
+int fgc_texture_release(fgc_texture* tex);
+
+/* ---- drawing ------------------------------------------------------------ */
+/* DrawMesh: all triangles, then all lines, in submission order; fragments
+ * resolve per pixel exactly as the reference's sequential DrawTriangle /
+ * DrawLine loop would. *info receives the summed RasterizeInfo. Blocks until
+ * the draw has finished. */
+int fgc_draw_mesh(fgc_context* ctx, const fgc_mesh* mesh, const fgc_state* st,
+                  const fgc_shader* sh, fgc_rasterize_info* info);
+/* DrawTriangles over mesh triangles [first, first+count). */
+int fgc_draw_triangles(fgc_context* ctx, const fgc_mesh* mesh, uint64_t first, uint64_t count,
+                       const fgc_state* st, const fgc_shader* sh, fgc_rasterize_info* info);
+/* DrawLines over mesh lines [first, first+count). */
+int fgc_draw_lines(fgc_context* ctx, const fgc_mesh* mesh, uint64_t first, uint64_t count,
+                   const fgc_state* st, const fgc_shader* sh, fgc_rasterize_info* info);
+
+/* ---- buffers ------------------------------------------------------------ */
+/* Copy the NRGBA colour buffer (width*height*4 bytes, rows top to bottom). */
+int fgc_read_color(fgc_context* ctx, uint8_t* nrgba);
+/* Copy the FP64 depth buffer (width*height values). */
+int fgc_read_depth(fgc_context* ctx, double* depth);
+/* Replace the colour / depth buffer from host memory. */
+int fgc_write_color(fgc_context* ctx, const uint8_t* nrgba);
+int fgc_write_depth(fgc_context* ctx, const double* depth);
+/* DepthImage (context.go:87-117): Gray16 normalisation of the depth buffer
+ * (width*height uint16 values). */
+int fgc_depth_image(fgc_context* ctx, uint16_t* gray16);
+/* Box-downsample the colour buffer by an integer factor on the device:
+ * out is (width/scale)*(height/scale)*4 bytes; each output channel is the
+ * rounded mean (sum + n/2) / n of the scale*scale input bytes. width and
+ * height must be multiples of scale. */
+int fgc_downsample(fgc_context* ctx, int32_t scale, uint8_t* out);
+/* Debug outputs (see fgc_context_set_debug). */
+int fgc_read_winner(fgc_context* ctx, uint32_t* winner);
+int fgc_read_shaded_color(fgc_context* ctx, double* rgba);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FAUXGLCUDA_H */

@@ -1,0 +1,180 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes access to the C restatement of the
+reference pipeline (oracle/fauxgl_oracle.c).
+
+Used by tests/ as the checker, by __graft_entry__.smoke() to check one small
+draw, and by bench.py's CPU-baseline leg. Never used by the product.
+
+Parity unpinned: the reference has no golden vectors for this path and cannot
+be built on either machine (no Go toolchain); the restatement is pinned by the
+hand-derived known-answer tests in tests/test_oracle_kat.py.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+from fauxgl_gb300 import _abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libfauxgl_oracle.so")
+_lib = None
+
+
+def build():
+    """Compile the oracle with its Makefile (gcc, -ffp-contract=off)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        build()
+    lib = ctypes.CDLL(LIB_PATH)
+    P = ctypes.c_void_p
+    D = ctypes.POINTER(ctypes.c_double)
+    U8 = ctypes.POINTER(ctypes.c_uint8)
+    U16 = ctypes.POINTER(ctypes.c_uint16)
+    lib.oracle_create.restype = P
+    lib.oracle_create.argtypes = [ctypes.c_int32, ctypes.c_int32]
+    lib.oracle_destroy.argtypes = [P]
+    lib.oracle_clear_color.argtypes = [P, D]
+    lib.oracle_clear_depth.argtypes = [P, ctypes.c_double]
+    lib.oracle_draw.restype = ctypes.c_int
+    lib.oracle_draw.argtypes = [P, ctypes.POINTER(_abi.FgcState), ctypes.POINTER(_abi.FgcShader), U16,
+                                ctypes.c_int32, ctypes.c_int32, D, D, D, D, ctypes.c_int64, ctypes.c_int64,
+                                D, D, D, D, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+                                ctypes.POINTER(_abi.FgcRasterizeInfo)]
+    for name, t in (("oracle_color", U8), ("oracle_depth", D), ("oracle_winner", ctypes.POINTER(ctypes.c_uint32)),
+                    ("oracle_shaded", D)):
+        getattr(lib, name).restype = t
+        getattr(lib, name).argtypes = [P]
+    lib.oracle_downsample.argtypes = [U8, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, U8]
+    lib.oracle_depth_image.argtypes = [P, U16]
+    lib.oracle_go_pow.restype = ctypes.c_double
+    lib.oracle_go_pow.argtypes = [ctypes.c_double, ctypes.c_double]
+    lib.oracle_nrgba.argtypes = [D, U8]
+    lib.oracle_blend.argtypes = [U8, D]
+    lib.oracle_clip_triangle.restype = ctypes.c_int
+    lib.oracle_clip_triangle.argtypes = [D, D]
+    _lib = lib
+    return lib
+
+
+def _d(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(
+        ctypes.POINTER(ctypes.c_double))
+
+
+class OracleContext:
+    """NewContext(width, height) on the CPU restatement."""
+
+    def __init__(self, width, height):
+        self.lib = load()
+        self.width, self.height = int(width), int(height)
+        self.h = self.lib.oracle_create(self.width, self.height)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.oracle_destroy(self.h)
+            self.h = None
+
+    def clear_color(self, rgba):
+        c = np.asarray(rgba, dtype=np.float64)
+        self.lib.oracle_clear_color(self.h, _d(c))
+
+    def clear_depth(self, value):
+        self.lib.oracle_clear_depth(self.h, float(value))
+
+    def draw(self, mesh, state, shader, texture=None, what=3, nthreads=0,
+             tri_range=None, line_range=None):
+        """Draw a Mesh with an fgc_state / fgc_shader pair; returns
+        (total_pixels, updated_pixels). what: 1 triangles, 2 lines, 3 both."""
+        keep = []
+
+        def arr(a):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            keep.append(a)
+            return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+        tf, tc = tri_range if tri_range is not None else (0, mesh.ntri)
+        lf, lc = line_range if line_range is not None else (0, mesh.nline)
+        tex_ptr, tw, th = None, 0, 0
+        if texture is not None:
+            t = np.ascontiguousarray(texture.texels, dtype=np.uint16)
+            keep.append(t)
+            tex_ptr = t.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16))
+            tw, th = texture.Width, texture.Height
+        info = _abi.FgcRasterizeInfo()
+        rc = self.lib.oracle_draw(self.h, ctypes.byref(state), ctypes.byref(shader), tex_ptr, tw, th,
+                                  arr(mesh.tri_pos), arr(mesh.tri_nrm), arr(mesh.tri_tex), arr(mesh.tri_col),
+                                  tf, tc, arr(mesh.line_pos), arr(mesh.line_nrm), arr(mesh.line_tex),
+                                  arr(mesh.line_col), lf, lc, what, nthreads, ctypes.byref(info))
+        if rc != 0:
+            raise RuntimeError("oracle_draw failed with status %d" % rc)
+        return int(info.total_pixels), int(info.updated_pixels)
+
+    def _view(self, fn, dtype, count):
+        p = fn(self.h)
+        return np.ctypeslib.as_array(p, shape=(count,)).astype(dtype, copy=True)
+
+    def color(self):
+        return self._view(self.lib.oracle_color, np.uint8, self.width * self.height * 4).reshape(
+            self.height, self.width, 4)
+
+    def depth(self):
+        return self._view(self.lib.oracle_depth, np.float64, self.width * self.height).reshape(
+            self.height, self.width)
+
+    def winner(self):
+        return self._view(self.lib.oracle_winner, np.uint32, self.width * self.height).reshape(
+            self.height, self.width)
+
+    def shaded(self):
+        return self._view(self.lib.oracle_shaded, np.float64, self.width * self.height * 4).reshape(
+            self.height, self.width, 4)
+
+    def depth_image(self):
+        out = np.empty(self.width * self.height, dtype=np.uint16)
+        self.lib.oracle_depth_image(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16)))
+        return out.reshape(self.height, self.width)
+
+
+def downsample(img, scale):
+    """Box downsample of an (H, W, 4) uint8 image (the project's definition)."""
+    lib = load()
+    img = np.ascontiguousarray(img, dtype=np.uint8)
+    h, w = img.shape[:2]
+    out = np.empty((h // scale, w // scale, 4), dtype=np.uint8)
+    lib.oracle_downsample(img.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), w, h, scale,
+                          out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+    return out
+
+
+def go_pow(x, y):
+    return load().oracle_go_pow(float(x), float(y))
+
+
+def nrgba(c):
+    out = np.zeros(4, dtype=np.uint8)
+    load().oracle_nrgba(_d(np.asarray(c, dtype=np.float64)), out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+    return tuple(int(v) for v in out)
+
+
+def blend(dst, src):
+    d = np.asarray(dst, dtype=np.uint8).copy()
+    s = np.asarray(src, dtype=np.float64)
+    load().oracle_blend(d.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), _d(s))
+    return tuple(int(v) for v in d)
+
+
+def clip_triangle(clip):
+    """ClipTriangle on clip-space outputs only: (3,4) -> (n,3,4)."""
+    c = np.ascontiguousarray(clip, dtype=np.float64).reshape(12)
+    out = np.zeros(7 * 3 * 4)
+    n = load().oracle_clip_triangle(_d(c), _d(out))
+    return out.reshape(7, 3, 4)[:n].copy()
