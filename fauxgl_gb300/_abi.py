@@ -67,6 +67,31 @@ class FgcShader(ctypes.Structure):
     ]
 
 
+FGC_STAGE_VERTEX, FGC_STAGE_SETUP, FGC_STAGE_CLIP, FGC_STAGE_BIN, FGC_STAGE_RASTER = range(5)
+FGC_STAGE_COUNT = 5
+STAGE_NAMES = ("vertex", "setup", "clip", "bin", "raster")
+
+
+class FgcStats(ctypes.Structure):
+    _fields_ = [
+        ("elements", ctypes.c_uint64),
+        ("unique_vertices", ctypes.c_uint64),
+        ("clipped", ctypes.c_uint64),
+        ("primitives", ctypes.c_uint64),
+        ("bin_entries", ctypes.c_uint64),
+        ("visited_pixels", ctypes.c_uint64),
+        ("covered_pixels", ctypes.c_uint64),
+        ("shaded_fragments", ctypes.c_uint64),
+        ("updated_pixels", ctypes.c_uint64),
+        ("kernel_launches", ctypes.c_uint64),
+        ("bands", ctypes.c_uint32),
+        ("band_rows", ctypes.c_uint32),
+        ("attempts", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
+        ("stage_ms", ctypes.c_double * FGC_STAGE_COUNT),
+    ]
+
+
 # Every exported symbol of include/fauxglcuda.h, with (restype, argtypes).
 _P = ctypes.c_void_p
 _PP = ctypes.POINTER(ctypes.c_void_p)
@@ -107,6 +132,9 @@ SIGNATURES = {
     "fgc_downsample": (_I, [_P, _I32, ctypes.POINTER(ctypes.c_uint8)]),
     "fgc_read_winner": (_I, [_P, ctypes.POINTER(ctypes.c_uint32)]),
     "fgc_read_shaded_color": (_I, [_P, _D]),
+    "fgc_context_set_timing": (_I, [_P, _I32]),
+    "fgc_context_last_stats": (_I, [_P, ctypes.POINTER(FgcStats)]),
+    "fgc_context_set_stream": (_I, [_P, _P]),
 }
 
 _lib = None

@@ -226,6 +226,24 @@ class Context:
         _abi.check(self._lib.fgc_downsample(self.handle, int(scale), out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))))
         return out
 
+    # -- instrumentation ----------------------------------------------------------
+    def SetTiming(self, enable):
+        """Record CUDA events between the pipeline stages of each draw."""
+        _abi.check(self._lib.fgc_context_set_timing(self.handle, int(bool(enable))))
+
+    def LastStats(self):
+        """Work counters and stage times (ms) of the last draw."""
+        st = _abi.FgcStats()
+        _abi.check(self._lib.fgc_context_last_stats(self.handle, ctypes.byref(st)))
+        d = {name: int(getattr(st, name)) for name, _ in _abi.FgcStats._fields_ if name != "stage_ms"}
+        d["stage_ms"] = {n: float(st.stage_ms[i]) for i, n in enumerate(_abi.STAGE_NAMES)}
+        return d
+
+    def SetStream(self, cuda_stream):
+        """Issue this context's work on a caller-owned CUDA stream handle (int
+        or None for the context's own stream)."""
+        _abi.check(self._lib.fgc_context_set_stream(self.handle, cuda_stream or None))
+
     # -- parity instrumentation -------------------------------------------------
     def SetDebug(self, flags):
         _abi.check(self._lib.fgc_context_set_debug(self.handle, int(flags)))

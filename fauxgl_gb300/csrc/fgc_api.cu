@@ -76,7 +76,7 @@ struct Counters {
     unsigned int band_counter;
     unsigned int tick_tri, tick_line, tick_scan, pad;
     unsigned long long tri_slots, line_slots, prim_total, pair_total;
-    unsigned long long info[2];
+    unsigned long long info[4];  // total, updated, visited, shaded
 };
 
 constexpr int kRasterThreads = 256;
@@ -145,7 +145,8 @@ struct fgc_mesh {
 struct fgc_context {
     int device = 0;
     int sms = 1;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;      // the stream work is issued on
+    cudaStream_t own_stream = nullptr;  // the context's own stream
     int32_t W = 0, H = 0;
     int64_t N = 0;
     DevBuf<uint32_t> color;
@@ -174,6 +175,9 @@ struct fgc_context {
     Counters* host_counters = nullptr;
     uint32_t clip_cap = 1024;
     uint64_t bin_cap = 0;
+    bool timing = false;
+    cudaEvent_t ev[FGC_STAGE_COUNT + 1] = {};
+    fgc_stats stats = {};
     std::mutex mu;
 };
 
@@ -283,9 +287,14 @@ int draw_shape(const fgc_context* c, DrawShape& s) {
     return FGC_OK;
 }
 
+void mark(fgc_context* c, int i) {
+    if (c->timing) cudaEventRecord(c->ev[i], c->stream);
+}
+
 int run_draw(fgc_context* c, const fgc_mesh* m, uint64_t tf, uint64_t tc, uint64_t lf, uint64_t lc,
              const StateView& sv, const ShaderView& shv, bool* retry) {
     *retry = false;
+    uint64_t launches = 0;
     DrawShape shape;
     int rc = draw_shape(c, shape);
     if (rc) return rc;
@@ -322,6 +331,7 @@ int run_draw(fgc_context* c, const fgc_mesh* m, uint64_t tf, uint64_t tc, uint64
     unsigned long long* t_scan = t_line + line_tiles + 1;
 
     const double w2 = (double)c->W / 2, h2 = (double)c->H / 2;
+    mark(c, 0);
     if (m->nuniq > 0 && (tc > 0 || lc > 0)) {
         VertexParams vp;
         vp.ux = m->ux.p;
@@ -337,7 +347,9 @@ int run_draw(fgc_context* c, const fgc_mesh* m, uint64_t tf, uint64_t tc, uint64
         vp.vout = c->vout.p;
         vertex_kernel<<<grid_for(m->nuniq, 256, c->sms * 16), 256, 0, c->stream>>>(vp);
         FGC_CUDA(cudaGetLastError());
+        launches++;
     }
+    mark(c, 1);
 
     GeomParams gp;
     memset(&gp, 0, sizeof(gp));
@@ -371,17 +383,28 @@ int run_draw(fgc_context* c, const fgc_mesh* m, uint64_t tf, uint64_t tc, uint64
     if (tc > 0) {
         setup_triangles_kernel<<<(unsigned)tri_tiles, 256, 0, c->stream>>>(gp);
         FGC_CUDA(cudaGetLastError());
-        clip_triangles_kernel<<<grid_for(c->clip_cap, 128, c->sms * 4), 128, 0, c->stream>>>(gp);
-        FGC_CUDA(cudaGetLastError());
+        launches++;
     }
     if (lc > 0) {
         setup_lines_kernel<<<(unsigned)line_tiles, 256, 0, c->stream>>>(gp);
         FGC_CUDA(cudaGetLastError());
+        launches++;
+    }
+    mark(c, 2);
+    if (tc > 0) {
+        clip_triangles_kernel<<<grid_for(c->clip_cap, 128, c->sms * 4), 128, 0, c->stream>>>(gp);
+        FGC_CUDA(cudaGetLastError());
+        launches++;
+    }
+    if (lc > 0) {
         clip_lines_kernel<<<grid_for(lc, 128, c->sms * 4), 128, 0, c->stream>>>(gp);
         FGC_CUDA(cudaGetLastError());
+        launches++;
     }
     prim_total_kernel<<<1, 1, 0, c->stream>>>(gp);
     FGC_CUDA(cudaGetLastError());
+    launches++;
+    mark(c, 3);
 
     BinParams bp;
     bp.pbox = c->pbox.p;
@@ -414,6 +437,8 @@ int run_draw(fgc_context* c, const fgc_mesh* m, uint64_t tf, uint64_t tc, uint64
         FGC_CUDA(cudaFuncSetAttribute(bin_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scat_smem));
     bin_scatter_kernel<<<shape.nblk, shape.bin_warps * 32, scat_smem, c->stream>>>(bp, shape.bin_warps);
     FGC_CUDA(cudaGetLastError());
+    launches += 3;
+    mark(c, 4);
 
     RasterParams rp;
     memset(&rp, 0, sizeof(rp));
@@ -455,10 +480,31 @@ int run_draw(fgc_context* c, const fgc_mesh* m, uint64_t tf, uint64_t tc, uint64
         rp.dbg = c->dbg.p;
     }
     FGC_CUDA(launch_raster(sv.precision, rgrid, kRasterThreads, shape.smem, c->stream, rp));
+    launches++;
+    mark(c, 5);
 
     FGC_CUDA(cudaMemcpyAsync(c->host_counters, c->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream));
     FGC_CUDA(cudaStreamSynchronize(c->stream));
     const Counters& hc = *c->host_counters;
+    fgc_stats& S = c->stats;
+    S.kernel_launches += launches;
+    S.attempts++;
+    S.elements = tc + lc;
+    S.unique_vertices = (tc > 0 || lc > 0) ? m->nuniq : 0;
+    S.clipped = (uint64_t)hc.clip_count + hc.lclip_count;
+    S.primitives = hc.prim_total;
+    S.bin_entries = hc.pair_total;
+    S.covered_pixels = hc.info[0];
+    S.updated_pixels = hc.info[1];
+    S.visited_pixels = hc.info[2];
+    S.shaded_fragments = hc.info[3];
+    S.bands = shape.nbands;
+    S.band_rows = (uint32_t)shape.R;
+    for (int i = 0; i < FGC_STAGE_COUNT; i++) {
+        float ms = 0;
+        if (c->timing) cudaEventElapsedTime(&ms, c->ev[i], c->ev[i + 1]);
+        S.stage_ms[i] = ms;
+    }
     if (hc.status & ST_LOOKBACK_TIMEOUT)
         return fail(FGC_ERR_DEVICE_LIMIT, "a look-back wait in the setup or scan stage timed out");
     if (hc.status & (ST_CLIP_OVERFLOW | ST_POOL_OVERFLOW)) {
@@ -490,6 +536,7 @@ int draw(fgc_context* c, const fgc_mesh* m, uint64_t tf, uint64_t tc, uint64_t l
     if (rc) return rc;
     std::lock_guard<std::mutex> lock(c->mu);
     FGC_CUDA(cudaSetDevice(c->device));
+    c->stats = fgc_stats{};
     for (int attempt = 0; attempt < 8; attempt++) {
         bool retry = false;
         rc = run_draw(c, m, tf, tc, lf, lc, sv, shv, &retry);
@@ -575,8 +622,13 @@ int fgc_context_create(int32_t width, int32_t height, fgc_context** out) {
     cudaError_t e = cudaGetDevice(&c->device);
     if (e != cudaSuccess) return bail(fail(FGC_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e)));
     cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
-    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return bail(fail(FGC_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)));
+    c->stream = c->own_stream;
+    for (int i = 0; i <= FGC_STAGE_COUNT; i++) {
+        e = cudaEventCreate(&c->ev[i]);
+        if (e != cudaSuccess) return bail(fail(FGC_ERR_CUDA, std::string("cudaEventCreate: ") + cudaGetErrorString(e)));
+    }
     c->W = width;
     c->H = height;
     c->N = (int64_t)width * height;
@@ -597,7 +649,9 @@ int fgc_context_destroy(fgc_context* c) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     if (c->host_counters) cudaFreeHost(c->host_counters);
-    cudaStreamDestroy(c->stream);
+    for (int i = 0; i <= FGC_STAGE_COUNT; i++)
+        if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
     return FGC_OK;
 }
@@ -617,6 +671,28 @@ int fgc_context_set_debug(fgc_context* c, int32_t flags) {
     int rc = ensure_debug(c);
     if (rc) return rc;
     FGC_CUDA(cudaStreamSynchronize(c->stream));
+    return FGC_OK;
+}
+
+int fgc_context_set_timing(fgc_context* c, int32_t enable) {
+    if (!c) return fail(FGC_ERR_INVALID_ARGUMENT, "null context");
+    std::lock_guard<std::mutex> lock(c->mu);
+    c->timing = enable != 0;
+    return FGC_OK;
+}
+
+int fgc_context_last_stats(const fgc_context* c, fgc_stats* out) {
+    if (!c || !out) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
+    *out = c->stats;
+    return FGC_OK;
+}
+
+int fgc_context_set_stream(fgc_context* c, void* cuda_stream) {
+    if (!c) return fail(FGC_ERR_INVALID_ARGUMENT, "null context");
+    std::lock_guard<std::mutex> lock(c->mu);
+    FGC_CUDA(cudaSetDevice(c->device));
+    FGC_CUDA(cudaStreamSynchronize(c->stream));
+    c->stream = cuda_stream ? (cudaStream_t)cuda_stream : c->own_stream;
     return FGC_OK;
 }
 

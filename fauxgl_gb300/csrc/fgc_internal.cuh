@@ -90,7 +90,7 @@ struct RasterParams {
     const PoolVertex* pool;
     unsigned int* band_counter;
     unsigned int* status;
-    unsigned long long* info;   // [0] total pixels, [1] updated pixels
+    unsigned long long* info;   // total, updated, visited pixels, shaded fragments
     uint32_t* winner;           // debug, or null
     double* shaded;             // debug, or null
     double* dbg;                // debug scratch: gridDim * F * 4 doubles

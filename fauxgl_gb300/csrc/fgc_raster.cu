@@ -377,7 +377,8 @@ __device__ __forceinline__ void walk_init(Walk& s, const RPrim& R, const PBox& b
 // Advance a walk, recording up to quota fragments. Returns the number of
 // covered in-band pixels (TotalPixels).
 __device__ __forceinline__ uint32_t walk_run(Walk& s, const RPrim& R, const RasterParams& P, const BandCtx& B,
-                                             RasterSmem& S, uint32_t* s_nfrag, uint32_t* s_conflict, int quota) {
+                                             RasterSmem& S, uint32_t* s_nfrag, uint32_t* s_conflict, int quota,
+                                             uint64_t& visited) {
     uint32_t total = 0;
     int rec = 0;
     const double bias = P.st.depth_bias;
@@ -389,6 +390,7 @@ __device__ __forceinline__ uint32_t walk_run(Walk& s, const RPrim& R, const Rast
         s.w1 = __dadd_rn(s.w1, R.a1);
         s.w2 = __dadd_rn(s.w2, R.a2);
         const int64_t x = s.x++;
+        visited++;
         if (b0 < 0 || b1 < 0 || b2 < 0) {
             if (s.was) {
                 s.done = true;
@@ -582,7 +584,7 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
 
     const bool early = P.st.read_depth && (!P.st.write_depth || P.st.depth_bias >= 0);
     const uint64_t pair_total = *P.pair_total;
-    uint64_t tot = 0, upd = 0;
+    uint64_t tot = 0, upd = 0, vis = 0, shd = 0;
 
     for (;;) {
         if (threadIdx.x == 0) s_band = atomicAdd(P.band_counter, 1u);
@@ -684,7 +686,7 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
                 if (big) {
                     if (threadIdx.x < nunit && !wk.done) {
                         const uint32_t pp = S.cprim[0];
-                        tot += walk_run(wk, P.prims[pp], P, B, S, &s_nfrag, &s_conflict, quota);
+                        tot += walk_run(wk, P.prims[pp], P, B, S, &s_nfrag, &s_conflict, quota, vis);
                     }
                 } else {
                     for (uint32_t u = threadIdx.x; u < nunit; u += blockDim.x) {
@@ -692,11 +694,12 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
                         const RPrim& R = P.prims[pp];
                         Walk w2;
                         walk_init(w2, R, P.pbox[pp], S.urow[u], P.W, (int32_t)u);
-                        tot += walk_run(w2, R, P, B, S, &s_nfrag, &s_conflict, 0x7fffffff);
+                        tot += walk_run(w2, R, P, B, S, &s_nfrag, &s_conflict, 0x7fffffff, vis);
                     }
                 }
                 __syncthreads();
                 const uint32_t nfrag = s_nfrag;
+                if (threadIdx.x == 0) shd += nfrag;
                 for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) shade_fragment<PREC>(P, S, f);
                 __syncthreads();
                 resolve_chunk(P, B, S, nfrag, s_conflict != 0, upd);
@@ -716,10 +719,14 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
     for (int o = 16; o > 0; o >>= 1) {
         tot += __shfl_down_sync(0xffffffffu, tot, o);
         upd += __shfl_down_sync(0xffffffffu, upd, o);
+        vis += __shfl_down_sync(0xffffffffu, vis, o);
+        shd += __shfl_down_sync(0xffffffffu, shd, o);
     }
     if ((threadIdx.x & 31) == 0) {
         if (tot) atomicAdd(&P.info[0], (unsigned long long)tot);
         if (upd) atomicAdd(&P.info[1], (unsigned long long)upd);
+        if (vis) atomicAdd(&P.info[2], (unsigned long long)vis);
+        if (shd) atomicAdd(&P.info[3], (unsigned long long)shd);
     }
 }
 

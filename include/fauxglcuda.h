@@ -203,6 +203,32 @@ int fgc_downsample(fgc_context* ctx, int32_t scale, uint8_t* out);
 int fgc_read_winner(fgc_context* ctx, uint32_t* winner);
 int fgc_read_shaded_color(fgc_context* ctx, double* rgba);
 
+/* ---- instrumentation (no reference counterpart) ------------------------- */
+/* Work counters and stage times of the context's last draw. Stage times are
+ * filled only while timing is on (fgc_context_set_timing): CUDA events
+ * recorded on the draw's stream between the pipeline stages. */
+enum { FGC_STAGE_VERTEX = 0, FGC_STAGE_SETUP = 1, FGC_STAGE_CLIP = 2, FGC_STAGE_BIN = 3,
+       FGC_STAGE_RASTER = 4, FGC_STAGE_COUNT = 5 };
+typedef struct fgc_stats {
+    uint64_t elements;          /* triangles + lines submitted                     */
+    uint64_t unique_vertices;   /* vertex-stage invocations (welded positions)     */
+    uint64_t clipped;           /* elements that went through clipping             */
+    uint64_t primitives;        /* raster primitive slots                          */
+    uint64_t bin_entries;       /* (primitive, band) pairs                         */
+    uint64_t visited_pixels;    /* pixels stepped by the edge walk                 */
+    uint64_t covered_pixels;    /* in-frame covered pixels (TotalPixels)           */
+    uint64_t shaded_fragments;  /* fragments shaded (after early depth rejection)  */
+    uint64_t updated_pixels;    /* UpdatedPixels                                   */
+    uint64_t kernel_launches;   /* kernels launched by the draw (all attempts)     */
+    uint32_t bands, band_rows, attempts, reserved;
+    double stage_ms[FGC_STAGE_COUNT];
+} fgc_stats;
+int fgc_context_set_timing(fgc_context* ctx, int32_t enable);
+int fgc_context_last_stats(const fgc_context* ctx, fgc_stats* out);
+/* Run the context's work on a caller-owned cudaStream_t (NULL restores the
+ * context's own stream). */
+int fgc_context_set_stream(fgc_context* ctx, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
