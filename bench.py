@@ -1,0 +1,464 @@
+#!/usr/bin/env python
+"""Benchmark of FauxGL's triangle pipeline on GB300.
+
+Workload (one step = one frame): the dense-mesh 1080p frame -- a displaced
+icosphere of 1,310,720 triangles fit to the bi-unit cube with normals
+smoothed at 30 degrees, 1920x1080, PhongShader (light (-0.75,1,0.25), object
+#468966), back-face culling, colour cleared to #FFF8E3 and depth to
+MaxFloat64 every frame. Seeded synthetic data (the reference's benchmark
+mesh, the Stanford Dragon, is not available).
+
+value   frames/s of the plain FP64 form (the reference's arithmetic, bit-exact
+        to it) with the mesh resident in HBM; CUDA events on the stream the
+        library launches on bracket the K timed frames.
+e2e     the same frames through the C ABI with a host readback each frame:
+        fgc_clear_color + fgc_clear_depth + fgc_draw_mesh + fgc_read_color
+        into pinned host memory (H2D: the draw-state and shader structs;
+        D2H: the NRGBA frame and RasterizeInfo).
+Also reported: the mixed form at 1x, both forms at 16x supersampling with the
+wireframe overlay and device box-downsample (7680x4320 -> 1920x1080), per-stage
+times, the roofline of the dominant stage, the CPU baseline, and the clocks
+sampled during the timed region.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "frames/s at 1.3M tris 1080p 1x/16xSS, mixed vs FP64-plain; batch p99 latency"
+WORKLOAD = ("dense-mesh 1080p frame: displaced icosphere 1,310,720 triangles (subdivision 8, seed 1), "
+            "1920x1080, PhongShader, back-face culling, colour+depth clear per frame")
+W, H = 1920, 1080
+SS = 4
+
+# Algorithmic FP64 operations (add, subtract, multiply, divide, sqrt: one
+# each; compares not counted) of the reference's rasterize loop
+# (context.go:184-278) per event, for the Phong shader with an object colour,
+# no texture and SpecularPower 32 (shader.go:75-96, vertex.go:18-47).
+FLOPS_PER_VISITED = 6        # b_k = w_k*ra (3), w_k += a_k (3)
+FLOPS_PER_COVERED = 6        # z (3 mul, 2 add), bz (1)
+FLOPS_PER_SHADED_PHONG = 119  # perspective 6, position 21, normal 31, Phong 61
+FLOPS_PER_SHADED_SOLID = 0
+# Triangle setup (drawClippedTriangle + rasterize prologue): NDC area per
+# triangle, edge setup per surviving primitive.
+FLOPS_SETUP_PER_TRIANGLE = 7
+FLOPS_SETUP_PER_PRIM = 40
+FLOPS_VERTEX_PER_UNIQUE = 34  # MulPositionW 24, NDC 3 divides, screen 6, 1/W
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--ss-steps", type=int, default=5, help="timed frames of the 16x supersampled variants")
+    ap.add_argument("--cpu-frames", type=int, default=5)
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
+        os.environ.get("LOCAL_RANK", "0"))
+
+
+def build_scene():
+    from fauxgl_gb300 import scenes
+    t = time.time()
+    mesh = scenes.displaced_sphere(8, seed=1)
+    log("scene: %d triangles in %.1fs" % (mesh.ntri, time.time() - t))
+    return mesh
+
+
+def phong_struct(w, h):
+    from fauxgl_gb300 import scenes
+    from fauxgl_gb300.shader import NewPhongShader, to_fgc_shader
+    sh = NewPhongShader(scenes.camera_matrix(w, h), scenes.LIGHT, scenes.EYE)
+    sh.ObjectColor = scenes.OBJECT_COLOR
+    return to_fgc_shader(sh)
+
+
+def overlay_struct(w, h):
+    from fauxgl_gb300 import scenes
+    from fauxgl_gb300.shader import NewSolidColorShader, to_fgc_shader
+    return to_fgc_shader(NewSolidColorShader(scenes.camera_matrix(w, h), (0, 0, 0, 0.5)))
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples taken while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.rows = []
+        if self.proc is None:
+            return False
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        for line in out.splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 9:
+                self.rows.append(parts)
+        return False
+
+    def summary(self):
+        rows = getattr(self, "rows", [])
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows),
+                "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit()) if rows else None}
+
+
+class Frame:
+    """A context plus the draws of one benchmark frame."""
+
+    def __init__(self, lib, mesh_h, w, h, precision, overlay=False, scale=1):
+        from fauxgl_gb300 import _abi, scenes
+        self.lib, self.mesh_h, self.w, self.h = lib, mesh_h, w, h
+        self.ctx = ctypes.c_void_p()
+        _abi.check(lib.fgc_context_create(w, h, ctypes.byref(self.ctx)))
+        self.st = _abi.FgcState()
+        lib.fgc_state_default(ctypes.byref(self.st))
+        self.st.precision = precision
+        self.sh = phong_struct(w, h)
+        self.overlay = overlay
+        if overlay:
+            self.st2 = _abi.FgcState.from_buffer_copy(self.st)
+            self.st2.wireframe = 1
+            self.st2.depth_bias = 1e-5
+            self.sh2 = overlay_struct(w, h)
+        self.scale = scale
+        self.bg = (ctypes.c_double * 4)(*scenes.BACKGROUND)
+        self.info = _abi.FgcRasterizeInfo()
+        self.ds = None
+        if scale > 1:
+            import numpy as np
+            self.ds = np.empty((h // scale, w // scale, 4), dtype=np.uint8)
+
+    def set_stream(self, stream):
+        from fauxgl_gb300 import _abi
+        _abi.check(self.lib.fgc_context_set_stream(self.ctx, stream))
+
+    def set_timing(self, on):
+        self.lib.fgc_context_set_timing(self.ctx, int(on))
+
+    def stats(self):
+        from fauxgl_gb300 import _abi
+        s = _abi.FgcStats()
+        _abi.check(self.lib.fgc_context_last_stats(self.ctx, ctypes.byref(s)))
+        return s
+
+    def run(self):
+        from fauxgl_gb300 import _abi
+        lib = self.lib
+        _abi.check(lib.fgc_clear_color(self.ctx, self.bg))
+        _abi.check(lib.fgc_clear_depth(self.ctx, 1.7976931348623157e308))
+        _abi.check(lib.fgc_draw_mesh(self.ctx, self.mesh_h, ctypes.byref(self.st), ctypes.byref(self.sh),
+                                     ctypes.byref(self.info)))
+        launches = self.stats().kernel_launches
+        if self.overlay:
+            _abi.check(lib.fgc_draw_mesh(self.ctx, self.mesh_h, ctypes.byref(self.st2), ctypes.byref(self.sh2),
+                                         ctypes.byref(self.info)))
+            launches += self.stats().kernel_launches
+        if self.ds is not None:
+            _abi.check(lib.fgc_downsample(self.ctx, self.scale,
+                                          self.ds.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))))
+            launches += 1
+        return launches
+
+    def close(self):
+        self.lib.fgc_context_destroy(self.ctx)
+
+
+def time_frames(frame, steps, warmup, torch, dist_barrier, stage_acc=None):
+    """Device-timed frames on torch's current stream (the library launches on
+    it). Returns (ms per frame, launches per frame)."""
+    stream = torch.cuda.current_stream()
+    frame.set_stream(stream.cuda_stream)
+    for _ in range(warmup):
+        frame.run()
+    dist_barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    launches = 0
+    e0.record(stream)
+    for _ in range(steps):
+        launches += frame.run()
+        if stage_acc is not None:
+            s = frame.stats()
+            for i in range(5):
+                stage_acc[i] += s.stage_ms[i]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    dist_barrier()
+    return e0.elapsed_time(e1) / steps, launches // max(steps, 1)
+
+
+def cpu_frames(mesh, nframes, nthreads):
+    """The oracle's threaded form (the reference's own worker split) on the
+    host cores: one warm-up frame, then the median of nframes."""
+    from fauxgl_gb300 import _abi, scenes
+    from oracle import oracle as O
+    st = _abi.FgcState()
+    _abi.load_library().fgc_state_default(ctypes.byref(st))
+    sh = phong_struct(W, H)
+    ctx = O.OracleContext(W, H)
+    times = []
+    for i in range(nframes + 1):
+        ctx.clear_color(scenes.BACKGROUND)
+        ctx.clear_depth(1.7976931348623157e308)
+        t = time.perf_counter()
+        ctx.draw(mesh, st, sh, nthreads=nthreads)
+        dt = time.perf_counter() - t
+        if i > 0:
+            times.append(dt)
+    return statistics.median(times), times
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the raster kernel from the committed ncu
+    summary (a 'traffic_bytes_per_launch: N' line), or None."""
+    p = os.path.join(ROOT, "profiles", "raster_kernel_dense1080p.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return int(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    nthreads = os.cpu_count() or 1
+    mesh = build_scene()
+    from fauxgl_gb300 import _abi, scenes
+    from oracle import oracle as O
+    st = _abi.FgcState()
+    _abi.load_library().fgc_state_default(ctypes.byref(st))
+    sh = phong_struct(W, H)
+    ctx = O.OracleContext(W, H)
+
+    def frame():
+        ctx.clear_color(scenes.BACKGROUND)
+        ctx.clear_depth(1.7976931348623157e308)
+        ctx.draw(mesh, st, sh, nthreads=nthreads)
+
+    for _ in range(args.warmup):
+        frame()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        frame()
+    dt = (time.perf_counter() - t) / args.steps
+    fps = 1.0 / dt
+    out = {
+        "impl": "reference", "metric": METRIC, "value": round(fps, 3), "unit": "frames/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "form": "reference arithmetic (FP64)",
+                   "implementation": "C restatement of the reference's rasterizer run with the reference's own "
+                                     "worker split (i %% %d), 256 striped locks; no Go toolchain on this "
+                                     "machine" % nthreads},
+        "cpu_baseline": {"value": round(fps, 3), "unit": "frames/s", "cores": nthreads, "kind": "port",
+                         "sample": "%d frames after %d warm-up frames" % (args.steps, args.warmup)},
+        "e2e": {"value": round(fps, 3), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import numpy as np
+    import torch
+    from fauxgl_gb300 import _abi
+    from fauxgl_gb300.context import _upload_mesh
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+        def barrier():
+            dist.barrier()
+    else:
+        def barrier():
+            pass
+    lib = _abi.load_library()
+    mesh = build_scene()
+    mesh_h = _upload_mesh(mesh)
+    gops = ctypes.c_double()
+    _abi.check(lib.fgc_measure_fp64_rate(ctypes.byref(gops)))
+    fp64_peak_tflops = gops.value / 1e3
+
+    # ---- headline: plain FP64 at 1080p, mesh resident ------------------------
+    plain = Frame(lib, mesh_h, W, H, _abi.FGC_PRECISION_PLAIN)
+    plain.set_timing(True)
+    stage = [0.0] * 5
+    with ClockSampler(local) as clocks:
+        ms, launches = time_frames(plain, args.steps, args.warmup, torch, barrier, stage)
+    stage = [s / args.steps for s in stage]
+    st = plain.stats()
+    info = (plain.info.total_pixels, plain.info.updated_pixels)
+    plain.set_timing(False)
+
+    # ---- e2e through the C ABI with the frame read back each step -----------
+    pinned = torch.empty((H, W, 4), dtype=torch.uint8, pin_memory=True)
+    ptr = ctypes.cast(pinned.data_ptr(), ctypes.POINTER(ctypes.c_uint8))
+
+    def e2e_frame():
+        plain.run()
+        _abi.check(lib.fgc_read_color(plain.ctx, ptr))
+
+    for _ in range(args.warmup):
+        e2e_frame()
+    barrier()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_frame()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    h2d = ctypes.sizeof(_abi.FgcState) + ctypes.sizeof(_abi.FgcShader) + 2 * 32
+    d2h = W * H * 4 + ctypes.sizeof(_abi.FgcRasterizeInfo)
+
+    # ---- mixed form at 1080p ------------------------------------------------
+    mixed = Frame(lib, mesh_h, W, H, _abi.FGC_PRECISION_MIXED)
+    mixed_ms, _ = time_frames(mixed, args.steps, args.warmup, torch, barrier)
+
+    # ---- 16x supersampled frame + wireframe overlay + box downsample --------
+    ss = {}
+    for name, prec in (("plain", _abi.FGC_PRECISION_PLAIN), ("mixed", _abi.FGC_PRECISION_MIXED)):
+        f = Frame(lib, mesh_h, W * SS, H * SS, prec, overlay=True, scale=SS)
+        ss_ms, ss_launch = time_frames(f, args.ss_steps, 1, torch, barrier)
+        ss[name] = {"value": round(1e3 / ss_ms, 3), "unit": "frames/s", "ms_per_frame": round(ss_ms, 3)}
+        f.close()
+    mixed.close()
+
+    # ---- roofline of the dominant stage --------------------------------------
+    names = list(_abi.STAGE_NAMES)
+    dom = max(range(5), key=lambda i: stage[i])
+    if names[dom] == "raster":
+        flops = (FLOPS_PER_VISITED * st.visited_pixels + FLOPS_PER_COVERED * st.covered_pixels
+                 + FLOPS_PER_SHADED_PHONG * st.shaded_fragments + st.shaded_fragments)
+    elif names[dom] == "setup":
+        flops = FLOPS_SETUP_PER_TRIANGLE * st.elements + FLOPS_SETUP_PER_PRIM * st.primitives
+    elif names[dom] == "vertex":
+        flops = FLOPS_VERTEX_PER_UNIQUE * st.unique_vertices
+    else:
+        flops = 0
+    achieved = flops / (stage[dom] * 1e-3) / 1e12 if stage[dom] > 0 else 0.0
+    # HBM view of the raster stage: framebuffer store (fused clear) + bins +
+    # primitive records + per-fragment vertex attributes
+    raster_bytes = (W * H * 12 + st.bin_entries * (4 + 176 + 16) + st.shaded_fragments * 3 * 48)
+    traffic = profile_traffic()
+
+    # ---- CPU baseline (rank 0, N=1 only) ------------------------------------
+    cpu = None
+    if rank == 0 and world == 1 and args.cpu_frames > 0:
+        nthreads = os.cpu_count() or 1
+        cpu_dt, _ = cpu_frames(mesh, args.cpu_frames, nthreads)
+        cpu = {"value": round(1.0 / cpu_dt, 3), "unit": "frames/s", "cores": nthreads, "kind": "port",
+               "sample": "median of %d frames of this workload after 1 warm-up frame, the reference's "
+                         "worker split over %d threads" % (args.cpu_frames, nthreads)}
+
+    # max over ranks of the per-frame time
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms, e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms, e2e_ms = float(t[0]), float(t[1])
+    fps = world * 1e3 / ms
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": round(fps, 3), "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "form": "plain FP64 (bit-exact to the reference)",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (mesh ~300 MB + framebuffer 25 MB resident; L2 129 MB)",
+                       "rasterize_info": list(info)},
+            "e2e": {"value": round(world * 1e3 / e2e_ms, 3), "unit": "frames/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches * args.steps,
+            "roofline": {"bound": "fp64", "kernel": names[dom] + "_kernel", "achieved": round(achieved, 4),
+                         "peak": round(fp64_peak_tflops, 4), "unit": "TFLOP/s",
+                         "frac": round(achieved / fp64_peak_tflops, 4) if fp64_peak_tflops else None,
+                         "traffic": traffic, "peak_source": "measured FP64 add rate (fgc_measure_fp64_rate)",
+                         "hbm": {"achieved": round(raster_bytes / (stage[4] * 1e-3) / 1e9, 1) if stage[4] else None,
+                                 "peak": 6694.5, "unit": "GB/s", "kernel": "raster_kernel",
+                                 "peak_source": "MEASURED_PEAKS.json hbm_gbs"}},
+            "stages_ms": {n: round(v, 4) for n, v in zip(names, stage)},
+            "work": {"elements": st.elements, "unique_vertices": st.unique_vertices, "clipped": st.clipped,
+                     "primitives": st.primitives, "bin_entries": st.bin_entries,
+                     "visited_pixels": st.visited_pixels, "covered_pixels": st.covered_pixels,
+                     "shaded_fragments": st.shaded_fragments, "updated_pixels": st.updated_pixels},
+            "mixed": {"value": round(world * 1e3 / mixed_ms, 3), "unit": "frames/s", "dtype": "f64+f32"},
+            "ss16": ss,
+            "clocks": clocks.summary(),
+        }
+        if cpu is not None:
+            out["cpu_baseline"] = cpu
+        print(json.dumps(out), flush=True)
+    plain.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

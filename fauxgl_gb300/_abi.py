@@ -135,6 +135,7 @@ SIGNATURES = {
     "fgc_context_set_timing": (_I, [_P, _I32]),
     "fgc_context_last_stats": (_I, [_P, ctypes.POINTER(FgcStats)]),
     "fgc_context_set_stream": (_I, [_P, _P]),
+    "fgc_measure_fp64_rate": (_I, [_D]),
 }
 
 _lib = None

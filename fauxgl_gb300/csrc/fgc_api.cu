@@ -696,6 +696,42 @@ int fgc_context_set_stream(fgc_context* c, void* cuda_stream) {
     return FGC_OK;
 }
 
+int fgc_measure_fp64_rate(double* gops_per_s) {
+    if (!gops_per_s) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
+    int dev = 0, sms = 1;
+    FGC_CUDA(cudaGetDevice(&dev));
+    FGC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    DevBuf<double> out;
+    FGC_CUDA(out.ensure((size_t)blocks * threads));
+    cudaStream_t s;
+    FGC_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int r = 0; r < 4; r++) {
+        cudaEventRecord(e0, s);
+        fp64_rate_kernel<<<blocks, threads, 0, s>>>(out.p, 1e-9, 2e-9, iters);
+        cudaEventRecord(e1, s);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            cudaStreamDestroy(s);
+            return fail(FGC_ERR_CUDA, std::string("fp64 probe: ") + cudaGetErrorString(e));
+        }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (r > 0 && ms < best) best = ms;  // the first run warms up
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(s);
+    *gops_per_s = (double)blocks * threads * iters * 8 / (best * 1e-3) / 1e9;
+    return FGC_OK;
+}
+
 int fgc_clear_color(fgc_context* c, const double rgba[4]) {
     if (!c || !rgba) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
     std::lock_guard<std::mutex> lock(c->mu);

@@ -127,6 +127,7 @@ __global__ void weld_emit_kernel(const double* cp, const uint32_t* slot_of, cons
                                  uint32_t* corner_uniq);
 __global__ void attrs_kernel(const double* cp, const double* nrm, uint64_t n, APosNrm64* pn64, APosNrm32* pn32);
 __global__ void f64_to_f32_kernel(const double* in, uint64_t n, float* out);
+__global__ void fp64_rate_kernel(double* out, double a, double b, int iters);
 
 // Dynamic shared memory of the raster kernel (layout in fgc_raster.cu):
 // depth[L] f64, b0/b1/b2/z[F] f64, scratch 64 u64, colour[L] u32,

@@ -166,6 +166,17 @@ __global__ void attrs_kernel(const double* cp, const double* nrm, uint64_t n, AP
     }
 }
 
+// FP64 pipe throughput probe: eight independent add chains per thread.
+__global__ void fp64_rate_kernel(double* out, double a, double b, int iters) {
+    double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
+           x7 = x0 + 7;
+    for (int i = 0; i < iters; i++) {
+        x0 = __dadd_rn(x0, a); x1 = __dadd_rn(x1, b); x2 = __dadd_rn(x2, a); x3 = __dadd_rn(x3, b);
+        x4 = __dadd_rn(x4, a); x5 = __dadd_rn(x5, b); x6 = __dadd_rn(x6, a); x7 = __dadd_rn(x7, b);
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
 __global__ void f64_to_f32_kernel(const double* in, uint64_t n, float* out) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
         out[i] = (float)in[i];

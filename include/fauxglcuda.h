@@ -228,6 +228,11 @@ int fgc_context_last_stats(const fgc_context* ctx, fgc_stats* out);
 /* Run the context's work on a caller-owned cudaStream_t (NULL restores the
  * context's own stream). */
 int fgc_context_set_stream(fgc_context* ctx, void* cuda_stream);
+/* FP64 pipe throughput of the current device, measured: independent FP64
+ * adds issued on every SM, in G instructions per second. It is the roofline
+ * denominator of the FP64-bound stages (one add, multiply or compare is one
+ * instruction). */
+int fgc_measure_fp64_rate(double* gops_per_s);
 
 #ifdef __cplusplus
 }
