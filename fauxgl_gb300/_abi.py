@@ -129,6 +129,7 @@ SIGNATURES = {
     "fgc_write_color": (_I, [_P, ctypes.POINTER(ctypes.c_uint8)]),
     "fgc_write_depth": (_I, [_P, _D]),
     "fgc_depth_image": (_I, [_P, ctypes.POINTER(ctypes.c_uint16)]),
+    "fgc_depth_image_noalloc": (_I, [_P, ctypes.POINTER(ctypes.c_uint16)]),
     "fgc_downsample": (_I, [_P, _I32, ctypes.POINTER(ctypes.c_uint8)]),
     "fgc_read_winner": (_I, [_P, ctypes.POINTER(ctypes.c_uint32)]),
     "fgc_read_shaded_color": (_I, [_P, _D]),

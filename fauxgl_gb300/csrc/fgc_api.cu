@@ -1026,3 +1026,76 @@ int fgc_read_shaded_color(fgc_context* c, double* rgba) {
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// DepthImage without device allocation.
+//
+// fgc_depth_image above grows c->lohi and c->gray with cudaMalloc the first
+// time it runs. Callers that may not let the library allocate device memory
+// once they are running (a service that reserves all its buffers before it
+// admits work, a host application that owns the GPU memory of its plugins)
+// use fgc_depth_image_noalloc instead: the same two kernels, with the
+// min/max pair and the Gray16 staging image placed in the static array
+// below. The array is reserved on every GPU that loads the library until the
+// process exits, which is why it is kept to 16 MiB: frames up to
+// FGC_DEPTH_IMAGE_NOALLOC_MAX_PIXELS (2^23) pixels.
+//
+// Host code cannot use the array's name as a device address; the first call
+// on each device, with that device current, looks the address up with
+// cudaGetSymbolAddress and keeps it (so that first call should come before
+// any stream capture). Every call re-initialises the min/max pair it needs,
+// and every call uses the same array, so calls that overlap on the GPU race.
+// ===========================================================================
+namespace {
+
+constexpr size_t kNoAllocPixels = FGC_DEPTH_IMAGE_NOALLOC_MAX_PIXELS;
+constexpr size_t kNoAllocBytes = 256 + kNoAllocPixels * sizeof(uint16_t);
+
+static __device__ __align__(256) unsigned char g_depth_image_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[256] = {};
+
+int noalloc_scratch(int device, unsigned char** out) {
+    if (device < 0 || device >= 256) return fail(FGC_ERR_UNSUPPORTED, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_depth_image_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(FGC_ERR_CUDA, std::string("cudaGetSymbolAddress(depth image scratch): ") +
+                                          cudaGetErrorString(e));
+        g_noalloc_ptr[device] = p;
+    }
+    *out = (unsigned char*)g_noalloc_ptr[device];
+    return FGC_OK;
+}
+
+}  // namespace
+
+extern "C" int fgc_depth_image_noalloc(fgc_context* c, uint16_t* gray16) {
+    if (!c || !gray16) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
+    if ((uint64_t)c->N > kNoAllocPixels)
+        return fail(FGC_ERR_INVALID_ARGUMENT,
+                    "fgc_depth_image_noalloc handles at most 8388608 pixels (its static scratch is 16 MiB); "
+                    "use fgc_depth_image for larger frames");
+    std::lock_guard<std::mutex> lock(c->mu);
+    FGC_CUDA(cudaSetDevice(c->device));
+    unsigned char* base = nullptr;
+    int rc = noalloc_scratch(c->device, &base);
+    if (rc) return rc;
+    rc = apply_pending_clears(c);
+    if (rc) return rc;
+    unsigned long long* lohi = (unsigned long long*)base;
+    uint16_t* gray = (uint16_t*)(base + 256);
+    // lo starts at the largest key, hi at the smallest (atomicMin / atomicMax)
+    FGC_CUDA(cudaMemsetAsync(lohi, 0xFF, sizeof(unsigned long long), c->stream));
+    FGC_CUDA(cudaMemsetAsync(lohi + 1, 0x00, sizeof(unsigned long long), c->stream));
+    int grid = grid_for((uint64_t)c->N, 256, c->sms * 8);
+    depth_minmax_kernel<<<grid, 256, 0, c->stream>>>(c->depth.p, (uint64_t)c->N, lohi);
+    depth_image_kernel<<<grid, 256, 0, c->stream>>>(c->depth.p, (uint64_t)c->N, lohi, gray);
+    FGC_CUDA(cudaGetLastError());
+    FGC_CUDA(cudaMemcpyAsync(gray16, gray, (size_t)c->N * 2, cudaMemcpyDeviceToHost, c->stream));
+    FGC_CUDA(cudaStreamSynchronize(c->stream));
+    return FGC_OK;
+}

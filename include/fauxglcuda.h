@@ -194,6 +194,19 @@ int fgc_write_depth(fgc_context* ctx, const double* depth);
 /* DepthImage (context.go:87-117): Gray16 normalisation of the depth buffer
  * (width*height uint16 values). */
 int fgc_depth_image(fgc_context* ctx, uint16_t* gray16);
+/* DepthImage without any device allocation (no counterpart in the
+ * reference). fgc_depth_image allocates its device staging buffers the first
+ * time it runs; a caller that must not have the library allocate GPU memory
+ * after start-up -- a render service that sizes every buffer before it admits
+ * requests, or a host application that owns the device memory of the plugins
+ * it loads -- calls this instead. The scratch is one static 16 MiB device
+ * array, reserved on every GPU that loads the library until the process
+ * exits, so frames are limited to FGC_DEPTH_IMAGE_NOALLOC_MAX_PIXELS pixels;
+ * larger contexts get FGC_ERR_INVALID_ARGUMENT. The first call on a device
+ * looks the array up on that device (make it before any stream capture).
+ * All calls share the array: calls that overlap on the GPU race. */
+#define FGC_DEPTH_IMAGE_NOALLOC_MAX_PIXELS 8388608
+int fgc_depth_image_noalloc(fgc_context* ctx, uint16_t* gray16);
 /* Box-downsample the colour buffer by an integer factor on the device:
  * out is (width/scale)*(height/scale)*4 bytes; each output channel is the
  * rounded mean (sum + n/2) / n of the scale*scale input bytes. width and
