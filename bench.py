@@ -67,6 +67,8 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ss-steps", type=int, default=5, help="timed frames of the 16x supersampled variants")
     ap.add_argument("--cpu-frames", type=int, default=5)
+    ap.add_argument("--only", choices=["all", "plain"], default="all",
+                    help="plain: time only the plain 1080p frame (for profiler runs)")
     return ap.parse_args()
 
 
@@ -169,6 +171,7 @@ class Frame:
             self.st2.depth_bias = 1e-5
             self.sh2 = overlay_struct(w, h)
         self.scale = scale
+        self.pass_ms = [[0.0] * 5, [0.0] * 5]  # stage times summed over runs: main pass, overlay
         self.bg = (ctypes.c_double * 4)(*scenes.BACKGROUND)
         self.info = _abi.FgcRasterizeInfo()
         self.ds = None
@@ -196,11 +199,15 @@ class Frame:
         _abi.check(lib.fgc_clear_depth(self.ctx, 1.7976931348623157e308))
         _abi.check(lib.fgc_draw_mesh(self.ctx, self.mesh_h, ctypes.byref(self.st), ctypes.byref(self.sh),
                                      ctypes.byref(self.info)))
-        launches = self.stats().kernel_launches
+        s = self.stats()
+        launches = s.kernel_launches
+        self.pass_ms[0] = [a + b for a, b in zip(self.pass_ms[0], s.stage_ms)]
         if self.overlay:
             _abi.check(lib.fgc_draw_mesh(self.ctx, self.mesh_h, ctypes.byref(self.st2), ctypes.byref(self.sh2),
                                          ctypes.byref(self.info)))
-            launches += self.stats().kernel_launches
+            s = self.stats()
+            launches += s.kernel_launches
+            self.pass_ms[1] = [a + b for a, b in zip(self.pass_ms[1], s.stage_ms)]
         if self.ds is not None:
             _abi.check(lib.fgc_downsample(self.ctx, self.scale,
                                           self.ds.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))))
@@ -341,52 +348,61 @@ def main():
     fp64_peak_tflops = gops.value / 1e3
 
     # ---- headline: plain FP64 at 1080p, mesh resident ------------------------
+    # nvidia-smi samples the clocks over all GPU measurements below.
+    clocks = ClockSampler(local)
+    clocks.__enter__()
     plain = Frame(lib, mesh_h, W, H, _abi.FGC_PRECISION_PLAIN)
     plain.set_timing(True)
     stage = [0.0] * 5
-    with ClockSampler(local) as clocks:
-        ms, launches = time_frames(plain, args.steps, args.warmup, torch, barrier, stage)
+    ms, launches = time_frames(plain, args.steps, args.warmup, torch, barrier, stage)
     stage = [s / args.steps for s in stage]
     st = plain.stats()
     info = (plain.info.total_pixels, plain.info.updated_pixels)
     plain.set_timing(False)
 
-    # ---- e2e through the C ABI with the frame read back each step -----------
-    pinned = torch.empty((H, W, 4), dtype=torch.uint8, pin_memory=True)
-    ptr = ctypes.cast(pinned.data_ptr(), ctypes.POINTER(ctypes.c_uint8))
-
-    def e2e_frame():
-        plain.run()
-        _abi.check(lib.fgc_read_color(plain.ctx, ptr))
-
-    for _ in range(args.warmup):
-        e2e_frame()
-    barrier()
-    torch.cuda.synchronize()
-    stream = torch.cuda.current_stream()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        e2e_frame()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    barrier()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
+    e2e_ms = mixed_ms = None
+    ss = {}
     h2d = ctypes.sizeof(_abi.FgcState) + ctypes.sizeof(_abi.FgcShader) + 2 * 32
     d2h = W * H * 4 + ctypes.sizeof(_abi.FgcRasterizeInfo)
+    if args.only == "all":
+        # ---- e2e through the C ABI with the frame read back each step -------
+        pinned = torch.empty((H, W, 4), dtype=torch.uint8, pin_memory=True)
+        ptr = ctypes.cast(pinned.data_ptr(), ctypes.POINTER(ctypes.c_uint8))
 
-    # ---- mixed form at 1080p ------------------------------------------------
-    mixed = Frame(lib, mesh_h, W, H, _abi.FGC_PRECISION_MIXED)
-    mixed_ms, _ = time_frames(mixed, args.steps, args.warmup, torch, barrier)
+        def e2e_frame():
+            plain.run()
+            _abi.check(lib.fgc_read_color(plain.ctx, ptr))
 
-    # ---- 16x supersampled frame + wireframe overlay + box downsample --------
-    ss = {}
-    for name, prec in (("plain", _abi.FGC_PRECISION_PLAIN), ("mixed", _abi.FGC_PRECISION_MIXED)):
-        f = Frame(lib, mesh_h, W * SS, H * SS, prec, overlay=True, scale=SS)
-        ss_ms, ss_launch = time_frames(f, args.ss_steps, 1, torch, barrier)
-        ss[name] = {"value": round(1e3 / ss_ms, 3), "unit": "frames/s", "ms_per_frame": round(ss_ms, 3)}
-        f.close()
-    mixed.close()
+        for _ in range(args.warmup):
+            e2e_frame()
+        barrier()
+        torch.cuda.synchronize()
+        stream = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            e2e_frame()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        e2e_ms = e0.elapsed_time(e1) / args.steps
+
+        # ---- mixed form at 1080p --------------------------------------------
+        mixed = Frame(lib, mesh_h, W, H, _abi.FGC_PRECISION_MIXED)
+        mixed_ms, _ = time_frames(mixed, args.steps, args.warmup, torch, barrier)
+        mixed.close()
+
+        # ---- 16x supersampled frame + wireframe overlay + box downsample ----
+        for name, prec in (("plain", _abi.FGC_PRECISION_PLAIN), ("mixed", _abi.FGC_PRECISION_MIXED)):
+            f = Frame(lib, mesh_h, W * SS, H * SS, prec, overlay=True, scale=SS)
+            f.set_timing(True)
+            ss_ms, ss_launch = time_frames(f, args.ss_steps, 1, torch, barrier)
+            n = args.ss_steps + 1
+            ss[name] = {"value": round(1e3 / ss_ms, 3), "unit": "frames/s", "ms_per_frame": round(ss_ms, 3),
+                        "stages_ms": {"surface": {k: round(v / n, 3) for k, v in zip(_abi.STAGE_NAMES, f.pass_ms[0])},
+                                      "overlay": {k: round(v / n, 3) for k, v in zip(_abi.STAGE_NAMES, f.pass_ms[1])}}}
+            f.close()
+    clocks.__exit__(None, None, None)
 
     # ---- roofline of the dominant stage --------------------------------------
     names = list(_abi.STAGE_NAMES)
@@ -408,7 +424,7 @@ def main():
 
     # ---- CPU baseline (rank 0, N=1 only) ------------------------------------
     cpu = None
-    if rank == 0 and world == 1 and args.cpu_frames > 0:
+    if rank == 0 and world == 1 and args.cpu_frames > 0 and args.only == "all":
         nthreads = os.cpu_count() or 1
         cpu_dt, _ = cpu_frames(mesh, args.cpu_frames, nthreads)
         cpu = {"value": round(1.0 / cpu_dt, 3), "unit": "frames/s", "cores": nthreads, "kind": "port",
@@ -418,9 +434,11 @@ def main():
     # max over ranks of the per-frame time
     if world > 1:
         import torch.distributed as dist
-        t = torch.tensor([ms, e2e_ms], device="cuda")
+        t = torch.tensor([ms, e2e_ms or 0.0, mixed_ms or 0.0], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms, e2e_ms = float(t[0]), float(t[1])
+        ms = float(t[0])
+        e2e_ms = float(t[1]) if e2e_ms else None
+        mixed_ms = float(t[2]) if mixed_ms else None
     fps = world * 1e3 / ms
     if rank == 0:
         out = {
@@ -431,8 +449,8 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "inputs larger than L2 (mesh ~300 MB + framebuffer 25 MB resident; L2 129 MB)",
                        "rasterize_info": list(info)},
-            "e2e": {"value": round(world * 1e3 / e2e_ms, 3), "unit": "frames/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+            "e2e": ({"value": round(world * 1e3 / e2e_ms, 3), "unit": "frames/s", "h2d_bytes_per_step": h2d,
+                     "d2h_bytes_per_step": d2h} if e2e_ms else None),
             "gpu_launches": launches * args.steps,
             "roofline": {"bound": "fp64", "kernel": names[dom] + "_kernel", "achieved": round(achieved, 4),
                          "peak": round(fp64_peak_tflops, 4), "unit": "TFLOP/s",
@@ -446,7 +464,8 @@ def main():
                      "primitives": st.primitives, "bin_entries": st.bin_entries,
                      "visited_pixels": st.visited_pixels, "covered_pixels": st.covered_pixels,
                      "shaded_fragments": st.shaded_fragments, "updated_pixels": st.updated_pixels},
-            "mixed": {"value": round(world * 1e3 / mixed_ms, 3), "unit": "frames/s", "dtype": "f64+f32"},
+            "mixed": ({"value": round(world * 1e3 / mixed_ms, 3), "unit": "frames/s", "dtype": "f64+f32"}
+                      if mixed_ms else None),
             "ss16": ss,
             "clocks": clocks.summary(),
         }
