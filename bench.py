@@ -152,6 +152,11 @@ class ClockSampler:
                 "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit()) if rows else None}
 
 
+def work_dict(s):
+    return {k: int(getattr(s, k)) for k in ("elements", "clipped", "primitives", "bin_entries", "visited_pixels",
+                                            "covered_pixels", "shaded_fragments", "updated_pixels")}
+
+
 class Frame:
     """A context plus the draws of one benchmark frame."""
 
@@ -172,6 +177,7 @@ class Frame:
             self.sh2 = overlay_struct(w, h)
         self.scale = scale
         self.pass_ms = [[0.0] * 5, [0.0] * 5]  # stage times summed over runs: main pass, overlay
+        self.pass_work = [None, None]
         self.bg = (ctypes.c_double * 4)(*scenes.BACKGROUND)
         self.info = _abi.FgcRasterizeInfo()
         self.ds = None
@@ -202,12 +208,14 @@ class Frame:
         s = self.stats()
         launches = s.kernel_launches
         self.pass_ms[0] = [a + b for a, b in zip(self.pass_ms[0], s.stage_ms)]
+        self.pass_work[0] = work_dict(s)
         if self.overlay:
             _abi.check(lib.fgc_draw_mesh(self.ctx, self.mesh_h, ctypes.byref(self.st2), ctypes.byref(self.sh2),
                                          ctypes.byref(self.info)))
             s = self.stats()
             launches += s.kernel_launches
             self.pass_ms[1] = [a + b for a, b in zip(self.pass_ms[1], s.stage_ms)]
+            self.pass_work[1] = work_dict(s)
         if self.ds is not None:
             _abi.check(lib.fgc_downsample(self.ctx, self.scale,
                                           self.ds.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))))
@@ -400,7 +408,8 @@ def main():
             n = args.ss_steps + 1
             ss[name] = {"value": round(1e3 / ss_ms, 3), "unit": "frames/s", "ms_per_frame": round(ss_ms, 3),
                         "stages_ms": {"surface": {k: round(v / n, 3) for k, v in zip(_abi.STAGE_NAMES, f.pass_ms[0])},
-                                      "overlay": {k: round(v / n, 3) for k, v in zip(_abi.STAGE_NAMES, f.pass_ms[1])}}}
+                                      "overlay": {k: round(v / n, 3) for k, v in zip(_abi.STAGE_NAMES, f.pass_ms[1])}},
+                        "work": {"surface": f.pass_work[0], "overlay": f.pass_work[1]}}
             f.close()
     clocks.__exit__(None, None, None)
 

@@ -164,6 +164,7 @@ struct fgc_context {
     DevBuf<uint8_t> vout;
     DevBuf<RPrim> prims;
     DevBuf<PBox> pbox;
+    DevBuf<uint32_t> pspan;
     DevBuf<ulonglong2> clip_list, lclip_list;
     DevBuf<PoolVertex> pool;
     DevBuf<uint32_t> mat, off, bins;
@@ -311,6 +312,7 @@ int run_draw(fgc_context* c, const fgc_mesh* m, uint64_t tf, uint64_t tc, uint64
     FGC_CUDA(c->vout.ensure(m->nuniq + 1));
     FGC_CUDA(c->prims.ensure(prim_cap));
     FGC_CUDA(c->pbox.ensure(prim_cap));
+    FGC_CUDA(c->pspan.ensure(prim_cap));
     FGC_CUDA(c->clip_list.ensure(c->clip_cap));
     FGC_CUDA(c->pool.ensure((size_t)c->clip_cap * 21));
     FGC_CUDA(c->lclip_list.ensure(lc + 1));
@@ -367,6 +369,7 @@ int run_draw(fgc_context* c, const fgc_mesh* m, uint64_t tf, uint64_t tc, uint64
     gp.vout = c->vout.p;
     gp.prims = c->prims.p;
     gp.pbox = c->pbox.p;
+    gp.pspan = c->pspan.p;
     gp.prim_cap = prim_cap;
     gp.clip_list = c->clip_list.p;
     gp.clip_cap = c->clip_cap;
@@ -374,6 +377,12 @@ int run_draw(fgc_context* c, const fgc_mesh* m, uint64_t tf, uint64_t tc, uint64
     gp.lclip_list = c->lclip_list.p;
     gp.lclip_count = &dc->lclip_count;
     gp.pool = c->pool.p;
+    gp.attr_mask = 0;
+    if (shv.kind == FGC_SHADER_PHONG) {
+        gp.attr_mask |= kAttrPos | kAttrNrm;
+        if (shv.object_is_discard) gp.attr_mask |= kAttrCol;
+    }
+    if (shv.has_texture || shv.kind == FGC_SHADER_TEXTURE) gp.attr_mask |= kAttrTex;
     gp.tri_slots = &dc->tri_slots;
     gp.line_slots = &dc->line_slots;
     gp.prim_total = &dc->prim_total;
@@ -444,6 +453,7 @@ int run_draw(fgc_context* c, const fgc_mesh* m, uint64_t tf, uint64_t tc, uint64
     memset(&rp, 0, sizeof(rp));
     rp.prims = c->prims.p;
     rp.pbox = c->pbox.p;
+    rp.pspan = c->pspan.p;
     rp.bins = c->bins.p;
     rp.off = c->off.p;
     rp.pair_total = &dc->pair_total;
@@ -505,6 +515,8 @@ int run_draw(fgc_context* c, const fgc_mesh* m, uint64_t tf, uint64_t tc, uint64
         if (c->timing) cudaEventElapsedTime(&ms, c->ev[i], c->ev[i + 1]);
         S.stage_ms[i] = ms;
     }
+    if (hc.status & ST_RASTER_INTERNAL)
+        return fail(FGC_ERR_DEVICE_LIMIT, "the raster stage detected an internal inconsistency");
     if (hc.status & ST_LOOKBACK_TIMEOUT)
         return fail(FGC_ERR_DEVICE_LIMIT, "a look-back wait in the setup or scan stage timed out");
     if (hc.status & (ST_CLIP_OVERFLOW | ST_POOL_OVERFLOW)) {

@@ -111,42 +111,45 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(BinParams P, int warps
         }
     }
     __syncthreads();
-    // phase 3: stable scatter, 32 primitives per round in lane order
+    // phase 3: stable scatter. A round takes the warp's next 32 primitives
+    // (lane order = submission order), lays their (primitive, band) pairs out
+    // in that order, and places the pairs 32 at a time: within a group, the
+    // pairs of one band are ranked by lane with __match_any_sync, after the
+    // pairs of that band from earlier groups and rounds (mycnt).
+    __shared__ uint32_t s_off[8][33];
+    const unsigned lanes_lt = (1u << lane) - 1u;
     for (uint64_t rb = slo; rb < shi; rb += 32) {
         const uint64_t p = rb + lane;
         uint32_t bl = 1, bh = 0;
         bool has = (p < shi) && prim_bands(P, P.pbox[p], bl, bh);
-        if (!has) { bl = 1; bh = 0; }
         const uint32_t span = has ? (bh - bl + 1) : 0u;
-        const uint32_t maxspan = __reduce_max_sync(0xffffffffu, span);
-        for (uint32_t k = 0; k < maxspan; k++) {
-            const uint32_t b = bl + k;
-            const bool mine = k < span;
-            uint32_t rank = 0;
-            for (int l2 = 0; l2 < 32; l2++) {
-                uint32_t lo2 = __shfl_sync(0xffffffffu, bl, l2);
-                uint32_t hi2 = __shfl_sync(0xffffffffu, bh, l2);
-                if (mine && l2 < lane && lo2 <= b && b <= hi2) rank++;
-            }
-            if (mine) P.bins[mycnt[b] + rank] = (uint32_t)p;
+        uint32_t incl = span;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
         }
+        s_off[w][lane] = incl - span;
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
         __syncwarp();
-        for (uint32_t k = 0; k < maxspan; k++) {
-            const uint32_t b = bl + k;
-            const bool mine = k < span;
-            uint32_t rank = 0;
-            bool later = false;
-            for (int l2 = 0; l2 < 32; l2++) {
-                uint32_t lo2 = __shfl_sync(0xffffffffu, bl, l2);
-                uint32_t hi2 = __shfl_sync(0xffffffffu, bh, l2);
-                if (mine && lo2 <= b && b <= hi2) {
-                    if (l2 < lane) rank++;
-                    if (l2 > lane) later = true;
-                }
+        for (uint32_t q0 = 0; q0 < total; q0 += 32) {
+            const uint32_t q = q0 + lane;
+            const bool active = q < total;
+            // owner: the last lane whose first pair index is <= q
+            int lo = 0, hi = 31;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s_off[w][mid] <= q) lo = mid;
+                else hi = mid - 1;
             }
-            if (mine && !later) mycnt[b] += rank + 1;
+            const uint32_t obl = __shfl_sync(0xffffffffu, bl, lo);
+            const uint32_t b = active ? obl + (q - s_off[w][lo]) : 0xFFFFFFFFu;
+            const unsigned peers = __match_any_sync(0xffffffffu, b);
+            if (active) P.bins[mycnt[b] + __popc(peers & lanes_lt)] = (uint32_t)(rb + lo);
+            __syncwarp();
+            if (active && (peers >> lane) == 1u) mycnt[b] += __popc(peers);  // highest lane of the band
+            __syncwarp();
         }
-        __syncwarp();
     }
 }
 

@@ -26,6 +26,7 @@ enum : uint32_t {
     ST_BIN_OVERFLOW = 1u << 1,    // more (prim, band) pairs than the bin array holds
     ST_LOOKBACK_TIMEOUT = 1u << 2,// a decoupled look-back wait gave up
     ST_POOL_OVERFLOW = 1u << 3,   // clip vertex pool too small
+    ST_RASTER_INTERNAL = 1u << 4, // a raster invariant failed; the draw's output is not trusted
 };
 
 // Bounded spin: a look-back wait gives up after this many polls.
@@ -35,6 +36,9 @@ constexpr uint32_t kSpinLimit = 1u << 22;
 constexpr uint32_t kLineFlag = 0x80000000u;
 // Vertex references: bit 31 set = index into the clip vertex pool.
 constexpr uint32_t kPoolFlag = 0x80000000u;
+
+// Vertex attributes a draw's shader reads (clipping interpolates only these).
+enum : uint32_t { kAttrPos = 1, kAttrNrm = 2, kAttrTex = 4, kAttrCol = 8 };
 
 // Primitive bounding boxes beyond these limits produce no fragments (the same
 // rule as the oracle; the reference would loop ~2^63 times on them).
@@ -135,7 +139,9 @@ __device__ __forceinline__ int64_t go_f2i(double f) {
 
 __device__ __forceinline__ bool dnan(double x) { return x != x; }
 __device__ __forceinline__ bool dinf(double x) { return fabs(x) == __longlong_as_double(0x7ff0000000000000LL); }
-__device__ __forceinline__ bool dfinite(double x) { return fabs(x) < __longlong_as_double(0x7ff0000000000000LL); }
+__device__ __forceinline__ bool dfinite(double x) {
+    return ((unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull) < 0x7ff0000000000000ull;
+}
 
 // math.Min / math.Max (explicit special cases: CUDA's fmin/fmax drop NaN).
 __device__ __forceinline__ double go_min(double x, double y) {
@@ -155,6 +161,102 @@ __device__ __forceinline__ double go_clamp(double x, double lo, double hi) {
     if (x < lo) return lo;
     if (x > hi) return hi;
     return x;
+}
+
+// ---------------------------------------------------------------------------
+// Exact IEEE predicates on the integer pipe. GB300 issues FP64 adds at ~1/38
+// of its integer rate, so comparisons that decide coverage and Go's Min/Max
+// special cases are made on the bit patterns; each helper returns exactly
+// what the FP64 comparison would.
+// ---------------------------------------------------------------------------
+constexpr unsigned long long kAbsMask = 0x7fffffffffffffffull;
+constexpr unsigned long long kInfBits = 0x7ff0000000000000ull;
+
+__device__ __forceinline__ unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
+__device__ __forceinline__ bool bnan(unsigned long long b) { return (b & kAbsMask) > kInfBits; }
+// Total order on non-NaN doubles as unsigned keys (-0 sorts below +0).
+__device__ __forceinline__ unsigned long long okey(unsigned long long b) {
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+// math.Min / math.Max from the bits: -Inf (+Inf) wins, then NaN, then the
+// total order, which also gives Go's signed-zero results.
+__device__ __forceinline__ double go_min_i(double x, double y) {
+    const unsigned long long bx = dbits(x), by = dbits(y);
+    if (bx == 0xfff0000000000000ull || by == 0xfff0000000000000ull) return __longlong_as_double(0xfff0000000000000LL);
+    if (bnan(bx) || bnan(by)) return __longlong_as_double(0x7ff8000000000000LL);
+    return okey(bx) <= okey(by) ? x : y;
+}
+__device__ __forceinline__ double go_max_i(double x, double y) {
+    const unsigned long long bx = dbits(x), by = dbits(y);
+    if (bx == kInfBits || by == kInfBits) return __longlong_as_double(0x7ff0000000000000LL);
+    if (bnan(bx) || bnan(by)) return __longlong_as_double(0x7ff8000000000000LL);
+    return okey(bx) >= okey(by) ? x : y;
+}
+// math.Max(x, 0): NaN stays NaN, positive values stay, everything else is +0.
+__device__ __forceinline__ double go_max0(double x) {
+    const unsigned long long b = dbits(x);
+    if (bnan(b)) return x;
+    return ((b >> 63) == 0 && b != 0) ? x : 0.0;
+}
+// math.Min(x, 1): NaN stays NaN, values below 1 stay, the rest is 1.
+__device__ __forceinline__ double go_min1(double x) {
+    const unsigned long long b = dbits(x);
+    if (bnan(b)) return x;
+    return ((b >> 63) || b < 0x3ff0000000000000ull) ? x : 1.0;
+}
+// x == 0 (either sign).
+__device__ __forceinline__ bool dzero(double x) { return (dbits(x) & kAbsMask) == 0; }
+// x < 1 (NaN: false).
+__device__ __forceinline__ bool dlt1(double x) {
+    const unsigned long long b = dbits(x);
+    if (bnan(b)) return false;
+    return (b >> 63) || b < 0x3ff0000000000000ull;
+}
+// x > 0 (NaN and -0: false).
+__device__ __forceinline__ bool dgt0(double x) {
+    const unsigned long long b = dbits(x);
+    return (b >> 63) == 0 && b != 0 && !bnan(b);
+}
+
+// uint8(Clamp(c, 0, 1) * 255) (color.go:56-63): the clamp and the truncation
+// on the integer pipe, the one multiply in FP64. NaN gives 0.
+__device__ __forceinline__ uint32_t go_u8_of_unit_i(double c) {
+    const unsigned long long b = dbits(c);
+    if (bnan(b)) return 0;
+    if ((b >> 63) || b == 0) return 0;                // c <= 0 (or -0)
+    if (b >= 0x3ff0000000000000ull) return 255;       // c >= 1
+    const double v = __dmul_rn(c, 255.0);             // (0, 255)
+    const unsigned long long vb = dbits(v);
+    const int e = (int)((vb >> 52) & 0x7ff) - 1023;   // v < 255 so e <= 7
+    if (e < 0) return 0;
+    const unsigned long long m = (vb & 0x000fffffffffffffull) | 0x0010000000000000ull;
+    return (uint32_t)(m >> (52 - e));
+}
+__device__ __forceinline__ uint32_t nrgba_pack_i(double r, double g, double b, double a) {
+    return go_u8_of_unit_i(r) | (go_u8_of_unit_i(g) << 8) | (go_u8_of_unit_i(b) << 16) | (go_u8_of_unit_i(a) << 24);
+}
+
+// w * ra < 0, for the coverage test of rasterize (context.go:208-215). When
+// ra is finite-or-infinite, nonzero and at least 2^-511 in magnitude and
+// |w| >= 2^-511, the product is a nonzero non-NaN number whose sign is the
+// XOR of the signs, so the bits decide; w = ±0 gives ±0 (or NaN), never
+// negative. Anything else (tiny or NaN w, unusual ra) takes the FP64 product.
+struct RaSign {
+    unsigned long long sign;
+    bool simple;
+};
+__device__ __forceinline__ RaSign ra_sign(double ra) {
+    const unsigned long long b = dbits(ra), m = b & kAbsMask;
+    return RaSign{b >> 63, m >= 0x2000000000000000ull && m <= kInfBits};
+}
+__device__ __forceinline__ bool neg_product(double w, double ra, RaSign rs) {
+    const unsigned long long b = dbits(w), m = b & kAbsMask;
+    if (rs.simple) {
+        if (m >= 0x2000000000000000ull && m <= kInfBits) return (b >> 63) != rs.sign;
+        if (m == 0) return false;
+    }
+    return __dmul_rn(w, ra) < 0;
 }
 
 // uint8(clamp(c, 0, 1) * 255) (color.go:56-63); NaN gives 0.
@@ -302,7 +404,7 @@ __device__ __forceinline__ D3 cross3(D3 a, D3 b) {
 }
 // Vector.Normalize (vector.go:83-86): multiply by 1/sqrt(x*x + y*y + z*z).
 __device__ __forceinline__ D3 normalize3(D3 a) {
-    double r = __ddiv_rn(1.0, __dsqrt_rn(dot3(a, a)));
+    double r = __drcp_rn(__dsqrt_rn(dot3(a, a)));  // 1 / sqrt(...), correctly rounded
     return muls3(a, r);
 }
 

@@ -25,7 +25,7 @@ __global__ void __launch_bounds__(256) vertex_kernel(VertexParams P) {
         D3 n = ndc_of(c);
         P.vndc[u] = make_double2(n.x, n.y);
         D3 s = screen_of_ndc(n, P.w2, P.h2);
-        P.vscr[u] = VScreen{s.x, s.y, s.z, __ddiv_rn(1.0, c.w)};
+        P.vscr[u] = VScreen{s.x, s.y, s.z, __drcp_rn(c.w)};
     }
 }
 
@@ -58,10 +58,10 @@ __device__ void make_prim(const GeomParams& P, uint64_t slot, D3 s0, D3 s1, D3 s
         return;
     }
     // integer bounding box (Min/Max, Floor/Ceil, int())
-    double mnx = floor(go_min(s0.x, go_min(s1.x, s2.x)));
-    double mny = floor(go_min(s0.y, go_min(s1.y, s2.y)));
-    double mxx = ceil(go_max(s0.x, go_max(s1.x, s2.x)));
-    double mxy = ceil(go_max(s0.y, go_max(s1.y, s2.y)));
+    double mnx = floor(go_min_i(s0.x, go_min_i(s1.x, s2.x)));
+    double mny = floor(go_min_i(s0.y, go_min_i(s1.y, s2.y)));
+    double mxx = ceil(go_max_i(s0.x, go_max_i(s1.x, s2.x)));
+    double mxy = ceil(go_max_i(s0.y, go_max_i(s1.y, s2.y)));
     int64_t x0 = go_f2i(mnx), x1 = go_f2i(mxx), y0 = go_f2i(mny), y1 = go_f2i(mxy);
     const int64_t lim = 1LL << 30;
     if (x1 - x0 > kMaxExtent || y1 - y0 > kMaxExtent || x0 < -lim || x1 > lim || y0 < -lim || y1 > lim) {
@@ -81,16 +81,32 @@ __device__ void make_prim(const GeomParams& P, uint64_t slot, D3 s0, D3 s1, D3 s
     double b20 = __dsub_rn(s2.x, s0.x);
     R.a0 = a12; R.a1 = a20; R.a2 = a01;
     R.b0 = b12; R.b1 = b20; R.b2 = b01;
-    R.ra = __ddiv_rn(1.0, edge_fn(s0, s1, s2));
-    R.q0 = __ddiv_rn(1.0, a12);
-    R.q1 = __ddiv_rn(1.0, a20);
-    R.q2 = __ddiv_rn(1.0, a01);
+    R.ra = __drcp_rn(edge_fn(s0, s1, s2));  // 1 / x, correctly rounded
+    R.q0 = __drcp_rn(a12);
+    R.q1 = __drcp_rn(a20);
+    R.q2 = __drcp_rn(a01);
     R.z0 = s0.z; R.z1 = s1.z; R.z2 = s2.z;
     R.r0 = r0; R.r1 = r1; R.r2 = r2;
     R.v0 = v0; R.v1 = v1; R.v2 = v2;
     R.elem = elem;
     P.prims[slot] = R;
     P.pbox[slot] = PBox{(int32_t)x0, (int32_t)x1, (int32_t)y0, (int32_t)y1};
+    // A row's covered pixel centres lie on one horizontal chord of the
+    // triangle, so a row holds at most (widest chord) + 1 of them; +3 more
+    // cover rounding at both ends and in this estimate. The raster stage
+    // sizes its fragment chunks with this bound (and checks it).
+    double ya = s0.y, yb = s1.y, yc = s2.y, xa = s0.x, xb = s1.x, xc = s2.x, t;
+    if (ya > yb) { t = ya; ya = yb; yb = t; t = xa; xa = xb; xb = t; }
+    if (yb > yc) { t = yb; yb = yc; yc = t; t = xb; xb = xc; xc = t; }
+    if (ya > yb) { t = ya; ya = yb; yb = t; t = xa; xa = xb; xb = t; }
+    double chord = mxx - mnx;
+    if (yc > ya) {
+        const double xl = xa + (yb - ya) / (yc - ya) * (xc - xa);
+        chord = fmin(fabs(xb - xl), chord);
+    }
+    const double span = ceil(chord * (1.0 + 1e-9)) + 4.0;
+    const double bw = (double)(x1 - x0 + 1);
+    P.pspan[slot] = (uint32_t)(span < bw ? span : bw);
 }
 
 // line (context.go:283-294): a screen-space quad of width LineWidth as two
@@ -275,21 +291,39 @@ __device__ __forceinline__ double interp1(double a, double b, double c, D4 w) {
     return __dmul_rn(n, w.w);
 }
 
-// InterpolateVertexes (vertex.go:18-47).
-__device__ FullVertex interp_full(const FullVertex& a, const FullVertex& b, const FullVertex& c, D4 w) {
-    FullVertex v;
-    v.pos = d3(interp1(a.pos.x, b.pos.x, c.pos.x, w), interp1(a.pos.y, b.pos.y, c.pos.y, w),
-               interp1(a.pos.z, b.pos.z, c.pos.z, w));
-    v.nrm = normalize3(d3(interp1(a.nrm.x, b.nrm.x, c.nrm.x, w), interp1(a.nrm.y, b.nrm.y, c.nrm.y, w),
-                          interp1(a.nrm.z, b.nrm.z, c.nrm.z, w)));
-    v.tu = interp1(a.tu, b.tu, c.tu, w);
-    v.tv = interp1(a.tv, b.tv, c.tv, w);
-    v.tz = interp1(a.tz, b.tz, c.tz, w);
-    v.col = d4(interp1(a.col.x, b.col.x, c.col.x, w), interp1(a.col.y, b.col.y, c.col.y, w),
-               interp1(a.col.z, b.col.z, c.col.z, w), interp1(a.col.w, b.col.w, c.col.w, w));
-    v.out = d4(interp1(a.out.x, b.out.x, c.out.x, w), interp1(a.out.y, b.out.y, c.out.y, w),
-               interp1(a.out.z, b.out.z, c.out.z, w), interp1(a.out.w, b.out.w, c.out.w, w));
-    return v;
+// InterpolateVertexes (vertex.go:18-47), split so that the clip-space
+// Output (which decides culling) is formed first and the other attributes
+// only when the piece survives and the shader reads them: an attribute no
+// shader reads never reaches an output, so skipping it changes nothing.
+__device__ __forceinline__ D4 interp_out(const FullVertex& a, const FullVertex& b, const FullVertex& c, D4 w) {
+    return d4(interp1(a.out.x, b.out.x, c.out.x, w), interp1(a.out.y, b.out.y, c.out.y, w),
+              interp1(a.out.z, b.out.z, c.out.z, w), interp1(a.out.w, b.out.w, c.out.w, w));
+}
+
+__device__ void interp_attrs(FullVertex& v, const FullVertex& a, const FullVertex& b, const FullVertex& c, D4 w,
+                             uint32_t mask) {
+    if (mask & kAttrPos)
+        v.pos = d3(interp1(a.pos.x, b.pos.x, c.pos.x, w), interp1(a.pos.y, b.pos.y, c.pos.y, w),
+                   interp1(a.pos.z, b.pos.z, c.pos.z, w));
+    else
+        v.pos = d3(0, 0, 0);
+    if (mask & kAttrNrm)
+        v.nrm = normalize3(d3(interp1(a.nrm.x, b.nrm.x, c.nrm.x, w), interp1(a.nrm.y, b.nrm.y, c.nrm.y, w),
+                              interp1(a.nrm.z, b.nrm.z, c.nrm.z, w)));
+    else
+        v.nrm = d3(0, 0, 0);
+    if (mask & kAttrTex) {
+        v.tu = interp1(a.tu, b.tu, c.tu, w);
+        v.tv = interp1(a.tv, b.tv, c.tv, w);
+    } else {
+        v.tu = v.tv = 0.0;
+    }
+    v.tz = 0.0;
+    if (mask & kAttrCol)
+        v.col = d4(interp1(a.col.x, b.col.x, c.col.x, w), interp1(a.col.y, b.col.y, c.col.y, w),
+                   interp1(a.col.z, b.col.z, c.col.z, w), interp1(a.col.w, b.col.w, c.col.w, w));
+    else
+        v.col = d4(0, 0, 0, 0);
 }
 
 // FixNormals (triangle.go:46-58).
@@ -328,9 +362,10 @@ __global__ void __launch_bounds__(128) clip_triangles_kernel(GeomParams P) {
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
         ulonglong2 ent = P.clip_list[e];
         uint64_t t = ent.x, base = ent.y;
+        const uint32_t mask = P.attr_mask;
         FullVertex tv[3];
         for (int c = 0; c < 3; c++) tv[c] = load_corner(P, 3 * t + c);
-        fix_normals(tv[0], tv[1], tv[2]);  // NewTriangle(v1, v2, v3)
+        if (mask & kAttrNrm) fix_normals(tv[0], tv[1], tv[2]);  // NewTriangle(v1, v2, v3)
         D3 p1 = d3(tv[0].out.x, tv[0].out.y, tv[0].out.z);
         D3 p2 = d3(tv[1].out.x, tv[1].out.y, tv[1].out.z);
         D3 p3 = d3(tv[2].out.x, tv[2].out.y, tv[2].out.z);
@@ -363,15 +398,7 @@ __global__ void __launch_bounds__(128) clip_triangles_kernel(GeomParams P) {
             bw[1] = barycentric(p1, p2, p3, d3(in[i - 1].x, in[i - 1].y, in[i - 1].z));
             bw[2] = barycentric(p1, p2, p3, d3(in[i].x, in[i].y, in[i].z));
             FullVertex v[3];
-            for (int c = 0; c < 3; c++) v[c] = interp_full(tv[0], tv[1], tv[2], bw[c]);
-            fix_normals(v[0], v[1], v[2]);  // NewTriangle
-            uint32_t pref[3];
-            for (int c = 0; c < 3; c++) {
-                uint32_t pi = e * 21 + sub * 3 + c;
-                P.pool[pi] = PoolVertex{v[c].pos.x, v[c].pos.y, v[c].pos.z, v[c].nrm.x, v[c].nrm.y, v[c].nrm.z,
-                                        v[c].tu, v[c].tv, v[c].col.x, v[c].col.y, v[c].col.z, v[c].col.w};
-                pref[c] = kPoolFlag | pi;
-            }
+            for (int c = 0; c < 3; c++) v[c].out = interp_out(tv[0], tv[1], tv[2], bw[c]);
             // drawClippedTriangle (context.go:316-349)
             D3 n0 = ndc_of(v[0].out), n1 = ndc_of(v[1].out), n2 = ndc_of(v[2].out);
             int order = cull_decision(P.st, n0.x, n0.y, n1.x, n1.y, n2.x, n2.y);
@@ -380,14 +407,24 @@ __global__ void __launch_bounds__(128) clip_triangles_kernel(GeomParams P) {
                 for (int q = 0; q < per; q++) write_dead(P, slot + q);
                 continue;
             }
+            for (int c = 0; c < 3; c++) interp_attrs(v[c], tv[0], tv[1], tv[2], bw[c], mask);
+            if (mask & kAttrNrm) fix_normals(v[0], v[1], v[2]);  // NewTriangle
+            uint32_t pref[3];
+            for (int c = 0; c < 3; c++) {
+                uint32_t pi = e * 21 + sub * 3 + c;
+                if (mask)
+                    P.pool[pi] = PoolVertex{v[c].pos.x, v[c].pos.y, v[c].pos.z, v[c].nrm.x, v[c].nrm.y, v[c].nrm.z,
+                                            v[c].tu, v[c].tv, v[c].col.x, v[c].col.y, v[c].col.z, v[c].col.w};
+                pref[c] = kPoolFlag | pi;
+            }
             int i0 = 0, i2 = 2;
             if (order < 0) { i0 = 2; i2 = 0; }
             D3 nn[3] = {n0, n1, n2};
             D3 s0 = screen_of_ndc(nn[i0], P.w2, P.h2);
             D3 s1 = screen_of_ndc(nn[1], P.w2, P.h2);
             D3 s2 = screen_of_ndc(nn[i2], P.w2, P.h2);
-            emit_triangle(P, slot, s0, s1, s2, __ddiv_rn(1.0, v[i0].out.w), __ddiv_rn(1.0, v[1].out.w),
-                          __ddiv_rn(1.0, v[i2].out.w), pref[i0], pref[1], pref[i2], (uint32_t)t);
+            emit_triangle(P, slot, s0, s1, s2, __drcp_rn(v[i0].out.w), __drcp_rn(v[1].out.w),
+                          __drcp_rn(v[i2].out.w), pref[i0], pref[1], pref[i2], (uint32_t)t);
         }
         for (; sub < 7; sub++)
             for (int q = 0; q < per; q++) write_dead(P, base + (uint64_t)sub * per + q);

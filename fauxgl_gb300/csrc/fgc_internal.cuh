@@ -31,6 +31,7 @@ struct GeomParams {
     const uint8_t* vout;
     RPrim* prims;
     PBox* pbox;
+    uint32_t* pspan;            // per primitive: bound on covered pixels in one row
     uint64_t prim_cap;          // slots available in prims / pbox
     ulonglong2* clip_list;      // (triangle, first slot)
     uint32_t clip_cap;
@@ -38,6 +39,7 @@ struct GeomParams {
     ulonglong2* lclip_list;     // (line, first slot), line_count entries
     uint32_t* lclip_count;
     PoolVertex* pool;           // 21 per clip_list entry
+    uint32_t attr_mask;         // kAttr* bits the shader reads
     unsigned long long* tri_slots;
     unsigned long long* line_slots;
     unsigned long long* prim_total;
@@ -71,6 +73,7 @@ struct ScanParams {
 struct RasterParams {
     const RPrim* prims;
     const PBox* pbox;
+    const uint32_t* pspan;
     const uint32_t* bins;
     const uint32_t* off;        // bin offsets: band b starts at off[b * nblk]
     const unsigned long long* pair_total;
@@ -132,7 +135,7 @@ __global__ void fp64_rate_kernel(double* out, double a, double b, int iters);
 // Dynamic shared memory of the raster kernel (layout in fgc_raster.cu):
 // depth[L] f64, b0/b1/b2/z[F] f64, scratch 64 u64, colour[L] u32,
 // key/colour/unit-slot/unit-row[F] u32, chunk tables 3*threads u32,
-// conflict bitmap, flags[F] u8.
+// per-pixel list heads[L] u16 (padded to 4 B), list links[F] u16, flags[F] u8.
 __host__ __device__ inline size_t raster_smem_bytes(int64_t L, int F, int threads) {
     size_t b = 0;
     b += (size_t)L * 8;
@@ -141,7 +144,8 @@ __host__ __device__ inline size_t raster_smem_bytes(int64_t L, int F, int thread
     b += (size_t)L * 4;
     b += (size_t)F * 4 * 4;
     b += (size_t)threads * 4 * 3;
-    b += ((size_t)(L + 31) / 32) * 4;
+    b += ((size_t)(L + 1) / 2) * 4;
+    b += (size_t)F * 2;
     b += (size_t)F;
     return (b + 15) & ~(size_t)15;
 }

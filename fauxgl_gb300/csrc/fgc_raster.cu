@@ -47,8 +47,9 @@ struct RasterSmem {
     uint32_t* cprim; // [kRT] chunk slot -> primitive
     int32_t* cylo;   // [kRT]
     int32_t* cnrow;  // [kRT]
-    uint32_t* bm;    // conflict bitmap
-    uint8_t* fflag;  // [F] (stored in the high byte of uslot's sibling)
+    unsigned short* head;  // [L] per pixel: last fragment of its list (0xFFFF: none)
+    unsigned short* nxt;   // [F] per fragment: the previous fragment on its pixel
+    uint8_t* fflag;  // [F] discard / blend flags
     unsigned long long* scratch;
 };
 
@@ -143,7 +144,7 @@ __device__ D4 shade64(const RasterParams& P, const RPrim& R, double b0, double b
     if (S.kind == FGC_SHADER_SOLID_COLOR) return d4(S.color[0], S.color[1], S.color[2], S.color[3]);
     // perspective-correct barycentrics (context.go:236-237)
     D4 w = d4(__dmul_rn(b0, R.r0), __dmul_rn(b1, R.r1), __dmul_rn(b2, R.r2), 0.0);
-    w.w = __ddiv_rn(1.0, __dadd_rn(__dadd_rn(w.x, w.y), w.z));
+    w.w = __drcp_rn(__dadd_rn(__dadd_rn(w.x, w.y), w.z));
     if (S.kind == FGC_SHADER_TEXTURE) {
         double u0, v0, u1, v1, u2, v2;
         fetch_tex64(P, R.v0, u0, v0);
@@ -175,20 +176,20 @@ __device__ D4 shade64(const RasterParams& P, const RPrim& R, double b0, double b
     }
     D3 L = d3(S.light[0], S.light[1], S.light[2]);
     D4 light = d4(S.ambient[0], S.ambient[1], S.ambient[2], S.ambient[3]);
-    double diffuse = go_max(dot3(nrm, L), 0.0);
+    double diffuse = go_max0(dot3(nrm, L));
     light = add4(light, muls4(d4(S.diffuse[0], S.diffuse[1], S.diffuse[2], S.diffuse[3]), diffuse));
-    if (diffuse > 0 && S.power > 0) {
+    if (dgt0(diffuse) && S.power > 0) {
         D3 camera = normalize3(sub3(d3(S.eye[0], S.eye[1], S.eye[2]), pos));
         D3 negl = d3(-L.x, -L.y, -L.z);
         D3 reflected = sub3(negl, muls3(nrm, __dmul_rn(2.0, dot3(nrm, negl))));  // Reflect, vector.go:175-177
-        double specular = go_max(dot3(camera, reflected), 0.0);
-        if (specular > 0) {
+        double specular = go_max0(dot3(camera, reflected));
+        if (dgt0(specular)) {
             specular = go_pow(specular, S.power);
             light = add4(light, muls4(d4(S.specular[0], S.specular[1], S.specular[2], S.specular[3]), specular));
         }
     }
-    return d4(go_min(__dmul_rn(color.x, light.x), 1.0), go_min(__dmul_rn(color.y, light.y), 1.0),
-              go_min(__dmul_rn(color.z, light.z), 1.0), color.w);
+    return d4(go_min1(__dmul_rn(color.x, light.x)), go_min1(__dmul_rn(color.y, light.y)),
+              go_min1(__dmul_rn(color.z, light.z)), color.w);
 }
 
 // ---------------------------------------------------------------------------
@@ -382,16 +383,18 @@ __device__ __forceinline__ uint32_t walk_run(Walk& s, const RPrim& R, const Rast
     uint32_t total = 0;
     int rec = 0;
     const double bias = P.st.depth_bias;
+    const double ra = R.ra;
+    const RaSign rs = ra_sign(ra);
     while (s.x <= s.x1) {
-        double b0 = __dmul_rn(s.w0, R.ra);
-        double b1 = __dmul_rn(s.w1, R.ra);
-        double b2 = __dmul_rn(s.w2, R.ra);
-        s.w0 = __dadd_rn(s.w0, R.a0);
-        s.w1 = __dadd_rn(s.w1, R.a1);
-        s.w2 = __dadd_rn(s.w2, R.a2);
+        // b_k = w_k * ra is negative exactly when neg_product says so; the
+        // products themselves are formed only for pixels that are used.
+        const double w0 = s.w0, w1 = s.w1, w2 = s.w2;
+        s.w0 = __dadd_rn(w0, R.a0);
+        s.w1 = __dadd_rn(w1, R.a1);
+        s.w2 = __dadd_rn(w2, R.a2);
         const int64_t x = s.x++;
         visited++;
-        if (b0 < 0 || b1 < 0 || b2 < 0) {
+        if (neg_product(w0, ra, rs) || neg_product(w1, ra, rs) || neg_product(w2, ra, rs)) {
             if (s.was) {
                 s.done = true;
                 return total;
@@ -407,17 +410,30 @@ __device__ __forceinline__ uint32_t walk_run(Walk& s, const RPrim& R, const Rast
         }
         if (i < B.i0) continue;
         total++;
+        const double b0 = __dmul_rn(w0, ra);
+        const double b1 = __dmul_rn(w1, ra);
+        const double b2 = __dmul_rn(w2, ra);
         double z = __dadd_rn(__dadd_rn(__dmul_rn(b0, R.z0), __dmul_rn(b1, R.z1)), __dmul_rn(b2, R.z2));
         const int pix = (int)(i - B.i0);
         if (B.early && __dadd_rn(z, bias) > S.depth[pix]) continue;
         uint32_t slot = atomicAdd(s_nfrag, 1u);
+        if (slot >= (uint32_t)P.F) {  // the chunk's size bound did not hold: the chunk is redone
+            atomicOr(s_conflict, 2u);
+            continue;
+        }
         S.fb0[slot] = b0;
         S.fb1[slot] = b1;
         S.fb2[slot] = b2;
         S.fz[slot] = z;
         S.fkey[slot] = ((uint32_t)pix << 16) | (uint32_t)s.unit;
-        uint32_t bit = 1u << (pix & 31);
-        if (atomicOr(&S.bm[pix >> 5], bit) & bit) *s_conflict = 1;
+        // push onto the pixel's list; a non-empty list means a conflict
+        unsigned short old = S.head[pix], assumed;
+        do {
+            assumed = old;
+            old = atomicCAS(&S.head[pix], assumed, (unsigned short)slot);
+        } while (old != assumed);
+        S.nxt[slot] = old;
+        if (old != 0xFFFFu) atomicOr(s_conflict, 1u);
         if (++rec == quota) return total;
     }
     s.done = true;
@@ -475,9 +491,9 @@ __device__ __forceinline__ void shade_fragment(const RasterParams& P, RasterSmem
     if (PREC == FGC_PRECISION_PLAIN) {
         D4 col = shade64(P, R, b0, b1, b2);
         c[0] = col.x; c[1] = col.y; c[2] = col.z; c[3] = col.w;
-        if (col.x == 0 && col.y == 0 && col.z == 0 && col.w == 0) fl |= kFragDiscard;
-        if (P.st.alpha_blend && col.w < 1) fl |= kFragBlend;
-        packed = nrgba_pack(col.x, col.y, col.z, col.w);
+        if (dzero(col.x) && dzero(col.y) && dzero(col.z) && dzero(col.w)) fl |= kFragDiscard;
+        if (P.st.alpha_blend && dlt1(col.w)) fl |= kFragBlend;
+        packed = nrgba_pack_i(col.x, col.y, col.z, col.w);
     } else {
         float4 col = shade32(P, R, b0, b1, b2);
         c[0] = col.x; c[1] = col.y; c[2] = col.z; c[3] = col.w;
@@ -497,39 +513,48 @@ __device__ __forceinline__ void shade_fragment(const RasterParams& P, RasterSmem
     }
 }
 
+// Apply the chunk's fragments per pixel in (primitive, row) order. Every
+// fragment was pushed onto its pixel's list in A1 (head / nxt). Without
+// conflicts each list has one entry and all apply in parallel; otherwise the
+// thread holding a list's head applies that pixel's fragments by increasing
+// key (unit index), selecting the next key from the short list each time.
+// The lists are emptied for the next chunk as they are applied.
 __device__ void resolve_chunk(const RasterParams& P, const BandCtx& B, RasterSmem& S, uint32_t nfrag,
                               bool conflict, uint64_t& updated) {
     if (!conflict) {
-        for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) apply_fragment(P, B, S, f, updated);
+        for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) {
+            apply_fragment(P, B, S, f, updated);
+            S.head[S.fkey[f] >> 16] = 0xFFFFu;
+        }
         return;
     }
-    unsigned long long* keys = reinterpret_cast<unsigned long long*>(S.fb0);
-    uint32_t n2 = 1;
-    while (n2 < nfrag) n2 <<= 1;
-    for (uint32_t f = threadIdx.x; f < n2; f += blockDim.x)
-        keys[f] = (f < nfrag) ? (((unsigned long long)S.fkey[f] << 32) | f) : ~0ull;
-    __syncthreads();
-    for (uint32_t k = 2; k <= n2; k <<= 1) {
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            for (uint32_t i = threadIdx.x; i < n2; i += blockDim.x) {
-                uint32_t ixj = i ^ j;
-                if (ixj > i) {
-                    unsigned long long a = keys[i], b = keys[ixj];
-                    bool up = (i & k) == 0;
-                    if ((a > b) == up) {
-                        keys[i] = b;
-                        keys[ixj] = a;
-                    }
+    for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) {
+        const uint32_t pix = S.fkey[f] >> 16;
+        if (S.head[pix] != f) continue;  // not the list head
+        uint32_t last = 0;               // keys of one pixel differ in the unit (low 16 bits)
+        bool first = true;
+        // A list holds at most nfrag entries; every traversal is capped at
+        // that, and a list that does not end within it is reported instead
+        // of followed.
+        for (uint32_t picked = 0; picked < nfrag; picked++) {
+            uint32_t best = 0xFFFFFFFFu, bestf = 0xFFFFu, steps = 0;
+            for (uint32_t g = f; g != 0xFFFFu && g < nfrag; g = S.nxt[g]) {
+                if (++steps > nfrag) {
+                    atomicOr(P.status, ST_RASTER_INTERNAL);
+                    break;
+                }
+                const uint32_t k = S.fkey[g];
+                if ((first || k > last) && k < best) {
+                    best = k;
+                    bestf = g;
                 }
             }
-            __syncthreads();
+            if (bestf == 0xFFFFu) break;
+            apply_fragment(P, B, S, bestf, updated);
+            last = best;
+            first = false;
         }
-    }
-    for (uint32_t s = threadIdx.x; s < nfrag; s += blockDim.x) {
-        const uint32_t pix = (uint32_t)(keys[s] >> 48);
-        if (s > 0 && (uint32_t)(keys[s - 1] >> 48) == pix) continue;
-        for (uint32_t j = s; j < nfrag && (uint32_t)(keys[j] >> 48) == pix; j++)
-            apply_fragment(P, B, S, (uint32_t)(keys[j] & 0xffffffffu), updated);
+        S.head[pix] = 0xFFFFu;
     }
 }
 
@@ -574,7 +599,8 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
         S.cprim = (uint32_t*)q; q += kRT * 4;
         S.cylo = (int32_t*)q; q += kRT * 4;
         S.cnrow = (int32_t*)q; q += kRT * 4;
-        S.bm = (uint32_t*)q; q += ((L + 31) / 32) * 4;
+        S.head = (unsigned short*)q; q += ((L + 1) / 2) * 4;
+        S.nxt = (unsigned short*)q; q += (size_t)F * 2;
         S.fflag = (uint8_t*)q;
     }
     __shared__ uint32_t s_band, s_nfrag, s_conflict, s_nprim, s_nunit, s_big;
@@ -604,13 +630,18 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
         for (int j = threadIdx.x; j < npx; j += blockDim.x) {
             S.depth[j] = P.clear_depth_pending ? P.clear_depth : P.depth[B.i0 + j];
             S.color[j] = P.clear_color_pending ? P.clear_color : P.color[B.i0 + j];
+            S.head[j] = 0xFFFFu;
         }
         __syncthreads();
 
         uint64_t k = 0;
+        bool box_bound = false;  // size the next chunk by bounding boxes only
         while (k < bcount) {
             // ---- chunk formation: a prefix of the remaining bin whose
-            // fragment bound fits the buffer
+            // fragment bound fits the buffer. A row of a primitive holds at
+            // most pspan covered pixels (its widest chord, set up in
+            // make_prim); box_bound falls back to the bounding-box width
+            // after a chunk whose walk outgrew the buffer.
             uint32_t p = 0;
             PBox bx{1, 0, 1, 0};
             int32_t ylo = 0, nrows = 0;
@@ -621,6 +652,7 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
                 bx = P.pbox[p];
                 rows_in_band(bx, P.W, B.i0, B.i1, ylo, nrows);
                 int64_t wid = (int64_t)bx.x1 - bx.x0 + 1;
+                if (!box_bound && (int64_t)P.pspan[p] < wid) wid = P.pspan[p];
                 if (wid > L) wid = L;
                 bound = (uint64_t)nrows * (uint64_t)wid;
             }
@@ -681,12 +713,12 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
                     s_nfrag = 0;
                     s_conflict = 0;
                 }
-                for (int j = threadIdx.x; j < (npx + 31) / 32; j += blockDim.x) S.bm[j] = 0;
                 __syncthreads();
+                uint64_t tchunk = 0;
                 if (big) {
                     if (threadIdx.x < nunit && !wk.done) {
                         const uint32_t pp = S.cprim[0];
-                        tot += walk_run(wk, P.prims[pp], P, B, S, &s_nfrag, &s_conflict, quota, vis);
+                        tchunk += walk_run(wk, P.prims[pp], P, B, S, &s_nfrag, &s_conflict, quota, vis);
                     }
                 } else {
                     for (uint32_t u = threadIdx.x; u < nunit; u += blockDim.x) {
@@ -694,19 +726,33 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
                         const RPrim& R = P.prims[pp];
                         Walk w2;
                         walk_init(w2, R, P.pbox[pp], S.urow[u], P.W, (int32_t)u);
-                        tot += walk_run(w2, R, P, B, S, &s_nfrag, &s_conflict, 0x7fffffff, vis);
+                        tchunk += walk_run(w2, R, P, B, S, &s_nfrag, &s_conflict, 0x7fffffff, vis);
                     }
                 }
                 __syncthreads();
+                if (s_conflict & 2u) {  // overflow: nothing was applied; empty the lists, redo with box bounds
+                    const uint32_t nrec = min(s_nfrag, (uint32_t)F);
+                    for (uint32_t f = threadIdx.x; f < nrec; f += blockDim.x) S.head[S.fkey[f] >> 16] = 0xFFFFu;
+                    break;
+                }
+                tot += tchunk;
                 const uint32_t nfrag = s_nfrag;
                 if (threadIdx.x == 0) shd += nfrag;
                 for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) shade_fragment<PREC>(P, S, f);
                 __syncthreads();
-                resolve_chunk(P, B, S, nfrag, s_conflict != 0, upd);
+                resolve_chunk(P, B, S, nfrag, (s_conflict & 1u) != 0, upd);
                 __syncthreads();
                 const int more = big ? __syncthreads_or(threadIdx.x < nunit && !wk.done) : 0;
                 if (!more) break;
             }
+            const bool redo = (s_conflict & 2u) != 0;
+            __syncthreads();
+            if (redo && !box_bound) {  // one redo per chunk, with bounds that cannot fail
+                box_bound = true;
+                continue;
+            }
+            if (redo && threadIdx.x == 0) atomicOr(P.status, ST_RASTER_INTERNAL);
+            box_bound = false;
             k += nprim;
         }
         for (int j = threadIdx.x; j < npx; j += blockDim.x) {
