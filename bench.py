@@ -67,8 +67,9 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ss-steps", type=int, default=5, help="timed frames of the 16x supersampled variants")
     ap.add_argument("--cpu-frames", type=int, default=5)
-    ap.add_argument("--only", choices=["all", "plain"], default="all",
-                    help="plain: time only the plain 1080p frame (for profiler runs)")
+    ap.add_argument("--only", choices=["all", "plain", "ss16"], default="all",
+                    help="plain / ss16: time only the plain 1080p frame or the plain 16x supersampled frame "
+                         "(for profiler runs)")
     return ap.parse_args()
 
 
@@ -354,6 +355,13 @@ def main():
     gops = ctypes.c_double()
     _abi.check(lib.fgc_measure_fp64_rate(ctypes.byref(gops)))
     fp64_peak_tflops = gops.value / 1e3
+
+    if args.only == "ss16":
+        f = Frame(lib, mesh_h, W * SS, H * SS, _abi.FGC_PRECISION_PLAIN, overlay=True, scale=SS)
+        ss_ms, _ = time_frames(f, args.steps, args.warmup, torch, barrier)
+        print(json.dumps({"ss16_plain_ms_per_frame": round(ss_ms, 3), "steps": args.steps}), flush=True)
+        f.close()
+        return 0
 
     # ---- headline: plain FP64 at 1080p, mesh resident ------------------------
     # nvidia-smi samples the clocks over all GPU measurements below.

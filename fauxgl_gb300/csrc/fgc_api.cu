@@ -276,6 +276,12 @@ int draw_shape(const fgc_context* c, DrawShape& s) {
     if (s.nbands > (uint32_t)kMaxBands) return fail(FGC_ERR_UNSUPPORTED, "frame has too many bands");
     s.F = kFragCap;
     s.smem = raster_smem_bytes(s.L, s.F, kRasterThreads);
+    // two CTAs per SM (the register budget allows two) when a smaller
+    // fragment buffer makes them fit
+    while (s.smem > 112 * 1024 && s.F > 512) {
+        s.F -= 128;
+        s.smem = raster_smem_bytes(s.L, s.F, kRasterThreads);
+    }
     while (s.smem > 227 * 1024 && s.F > 256) {
         s.F /= 2;
         s.smem = raster_smem_bytes(s.L, s.F, kRasterThreads);

@@ -132,19 +132,23 @@ __global__ void attrs_kernel(const double* cp, const double* nrm, uint64_t n, AP
 __global__ void f64_to_f32_kernel(const double* in, uint64_t n, float* out);
 __global__ void fp64_rate_kernel(double* out, double a, double b, int iters);
 
+// Pixel buckets of the raster kernel's per-chunk fragment lists.
+constexpr int kRasterHeads = 2048;
+
 // Dynamic shared memory of the raster kernel (layout in fgc_raster.cu):
-// depth[L] f64, b0/b1/b2/z[F] f64, scratch 64 u64, colour[L] u32,
+// depth[L] f64, b0/b1/b2/z[F] f64, scratch 64 u64,
 // key/colour/unit-slot/unit-row[F] u32, chunk tables 3*threads u32,
-// per-pixel list heads[L] u16 (padded to 4 B), list links[F] u16, flags[F] u8.
+// bucket list heads[kRasterHeads] u16, list links[F] u16, flags[F] u8.
+// The colour buffer is not staged: the band's pixels are read and written in
+// global memory by the CTA that owns them.
 __host__ __device__ inline size_t raster_smem_bytes(int64_t L, int F, int threads) {
     size_t b = 0;
     b += (size_t)L * 8;
     b += (size_t)F * 8 * 4;
     b += 64 * 8;
-    b += (size_t)L * 4;
     b += (size_t)F * 4 * 4;
     b += (size_t)threads * 4 * 3;
-    b += ((size_t)(L + 1) / 2) * 4;
+    b += (size_t)kRasterHeads * 2;
     b += (size_t)F * 2;
     b += (size_t)F;
     return (b + 15) & ~(size_t)15;

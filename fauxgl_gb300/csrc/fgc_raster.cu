@@ -30,6 +30,8 @@
 namespace fgc {
 
 constexpr int kRT = 256;  // threads per raster CTA
+static_assert(kRasterHeads >= 2 * 1024 && (kRasterHeads & (kRasterHeads - 1)) == 0, "bucket count");
+__device__ __forceinline__ uint32_t bucket_of(uint32_t pix) { return pix & (kRasterHeads - 1); }
 constexpr uint8_t kFragDiscard = 1;
 constexpr uint8_t kFragBlend = 2;
 
@@ -39,7 +41,6 @@ struct RasterSmem {
     double* fb1;
     double* fb2;
     double* fz;
-    uint32_t* color; // [L]
     uint32_t* fkey;  // [F] (pixel << 16) | unit
     uint32_t* fcol;  // [F] NRGBA
     uint32_t* uslot; // [F] unit -> chunk slot, flags in bits 24..
@@ -47,8 +48,8 @@ struct RasterSmem {
     uint32_t* cprim; // [kRT] chunk slot -> primitive
     int32_t* cylo;   // [kRT]
     int32_t* cnrow;  // [kRT]
-    unsigned short* head;  // [L] per pixel: last fragment of its list (0xFFFF: none)
-    unsigned short* nxt;   // [F] per fragment: the previous fragment on its pixel
+    unsigned short* head;  // [kHeads] per pixel bucket: last fragment of its list (0xFFFF: none)
+    unsigned short* nxt;   // [F] per fragment: the previous fragment in its bucket
     uint8_t* fflag;  // [F] discard / blend flags
     unsigned long long* scratch;
 };
@@ -426,11 +427,13 @@ __device__ __forceinline__ uint32_t walk_run(Walk& s, const RPrim& R, const Rast
         S.fb2[slot] = b2;
         S.fz[slot] = z;
         S.fkey[slot] = ((uint32_t)pix << 16) | (uint32_t)s.unit;
-        // push onto the pixel's list; a non-empty list means a conflict
-        unsigned short old = S.head[pix], assumed;
+        // push onto the pixel's bucket list; a non-empty list means a
+        // possible conflict (same pixel or same bucket)
+        unsigned short* hd = &S.head[bucket_of((uint32_t)pix)];
+        unsigned short old = *hd, assumed;
         do {
             assumed = old;
-            old = atomicCAS(&S.head[pix], assumed, (unsigned short)slot);
+            old = atomicCAS(hd, assumed, (unsigned short)slot);
         } while (old != assumed);
         S.nxt[slot] = old;
         if (old != 0xFFFFu) atomicOr(s_conflict, 1u);
@@ -456,13 +459,16 @@ __device__ __forceinline__ void apply_fragment(const RasterParams& P, const Band
         updated++;
         if (P.st.write_depth) S.depth[pix] = z;
         if (P.st.write_color) {
+            // The colour buffer stays in global memory: the band is this
+            // CTA's alone and one thread applies all of a pixel's fragments.
+            uint32_t* cp = P.color + B.i0 + pix;
             if (fl & kFragBlend) {
-                S.color[pix] = blend_nrgba(S.color[pix], S.fcol[f]);
+                *cp = blend_nrgba(*cp, S.fcol[f]);
             } else {
                 // SetNRGBA(x, y, c) ignores points outside the image rectangle
                 const int64_t i = B.i0 + pix;
                 const int64_t x = i - (int64_t)S.urow[unit] * P.W;
-                if (x >= 0 && x < P.W) S.color[pix] = S.fcol[f];
+                if (x >= 0 && x < P.W) *cp = S.fcol[f];
             }
         }
         if (P.winner) {
@@ -514,24 +520,25 @@ __device__ __forceinline__ void shade_fragment(const RasterParams& P, RasterSmem
 }
 
 // Apply the chunk's fragments per pixel in (primitive, row) order. Every
-// fragment was pushed onto its pixel's list in A1 (head / nxt). Without
-// conflicts each list has one entry and all apply in parallel; otherwise the
-// thread holding a list's head applies that pixel's fragments by increasing
-// key (unit index), selecting the next key from the short list each time.
-// The lists are emptied for the next chunk as they are applied.
+// fragment was pushed onto its pixel bucket's list in A1 (head / nxt).
+// Without collisions each list has one entry and all apply in parallel;
+// otherwise the thread holding a list's head applies the bucket's fragments
+// by increasing key -- pixel, then unit -- selecting the next key from the
+// short list each time. The lists are emptied for the next chunk as they are
+// applied.
 __device__ void resolve_chunk(const RasterParams& P, const BandCtx& B, RasterSmem& S, uint32_t nfrag,
                               bool conflict, uint64_t& updated) {
     if (!conflict) {
         for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) {
             apply_fragment(P, B, S, f, updated);
-            S.head[S.fkey[f] >> 16] = 0xFFFFu;
+            S.head[bucket_of(S.fkey[f] >> 16)] = 0xFFFFu;
         }
         return;
     }
     for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) {
-        const uint32_t pix = S.fkey[f] >> 16;
+        const uint32_t pix = bucket_of(S.fkey[f] >> 16);  // the bucket
         if (S.head[pix] != f) continue;  // not the list head
-        uint32_t last = 0;               // keys of one pixel differ in the unit (low 16 bits)
+        uint32_t last = 0;               // keys in a bucket are distinct
         bool first = true;
         // A list holds at most nfrag entries; every traversal is capped at
         // that, and a list that does not end within it is reported instead
@@ -591,7 +598,6 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
         S.fb2 = (double*)q; q += (size_t)F * 8;
         S.fz = (double*)q; q += (size_t)F * 8;
         S.scratch = (unsigned long long*)q; q += 64 * 8;
-        S.color = (uint32_t*)q; q += L * 4;
         S.fkey = (uint32_t*)q; q += (size_t)F * 4;
         S.fcol = (uint32_t*)q; q += (size_t)F * 4;
         S.uslot = (uint32_t*)q; q += (size_t)F * 4;
@@ -599,7 +605,7 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
         S.cprim = (uint32_t*)q; q += kRT * 4;
         S.cylo = (int32_t*)q; q += kRT * 4;
         S.cnrow = (int32_t*)q; q += kRT * 4;
-        S.head = (unsigned short*)q; q += ((L + 1) / 2) * 4;
+        S.head = (unsigned short*)q; q += (size_t)kRasterHeads * 2;
         S.nxt = (unsigned short*)q; q += (size_t)F * 2;
         S.fflag = (uint8_t*)q;
     }
@@ -629,9 +635,9 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
         const int npx = (int)(B.i1 - B.i0);
         for (int j = threadIdx.x; j < npx; j += blockDim.x) {
             S.depth[j] = P.clear_depth_pending ? P.clear_depth : P.depth[B.i0 + j];
-            S.color[j] = P.clear_color_pending ? P.clear_color : P.color[B.i0 + j];
-            S.head[j] = 0xFFFFu;
+            if (P.clear_color_pending) P.color[B.i0 + j] = P.clear_color;  // fused clear
         }
+        for (int j = threadIdx.x; j < kRasterHeads; j += blockDim.x) S.head[j] = 0xFFFFu;
         __syncthreads();
 
         uint64_t k = 0;
@@ -732,7 +738,8 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
                 __syncthreads();
                 if (s_conflict & 2u) {  // overflow: nothing was applied; empty the lists, redo with box bounds
                     const uint32_t nrec = min(s_nfrag, (uint32_t)F);
-                    for (uint32_t f = threadIdx.x; f < nrec; f += blockDim.x) S.head[S.fkey[f] >> 16] = 0xFFFFu;
+                    for (uint32_t f = threadIdx.x; f < nrec; f += blockDim.x)
+                        S.head[bucket_of(S.fkey[f] >> 16)] = 0xFFFFu;
                     break;
                 }
                 tot += tchunk;
@@ -755,10 +762,7 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
             box_bound = false;
             k += nprim;
         }
-        for (int j = threadIdx.x; j < npx; j += blockDim.x) {
-            P.depth[B.i0 + j] = S.depth[j];
-            P.color[B.i0 + j] = S.color[j];
-        }
+        for (int j = threadIdx.x; j < npx; j += blockDim.x) P.depth[B.i0 + j] = S.depth[j];
         __syncthreads();
     }
     // per-CTA counters
