@@ -17,6 +17,7 @@ FGC_ERR_CUDA = 3
 FGC_ERR_OUT_OF_MEMORY = 4
 FGC_ERR_DEVICE_LIMIT = 5
 FGC_ERR_UNSUPPORTED = 6
+FGC_ERR_BUSY = 7
 
 FGC_FACE_CW = 1
 FGC_FACE_CCW = 2
@@ -92,6 +93,31 @@ class FgcStats(ctypes.Structure):
     ]
 
 
+class FgcBatchItem(ctypes.Structure):
+    _fields_ = [
+        ("context", ctypes.c_void_p),
+        ("mesh", ctypes.c_void_p),
+        ("tri_first", ctypes.c_uint64),
+        ("tri_count", ctypes.c_uint64),
+        ("line_first", ctypes.c_uint64),
+        ("line_count", ctypes.c_uint64),
+        ("state", ctypes.POINTER(FgcState)),
+        ("shader", ctypes.POINTER(FgcShader)),
+        ("out_nrgba", ctypes.c_void_p),
+        ("out_scale", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
+class FgcBatchTuning(ctypes.Structure):
+    _fields_ = [
+        ("band_pixels", ctypes.c_int32),
+        ("prims_per_bin_block", ctypes.c_int32),
+        ("fragment_cap", ctypes.c_int32),
+        ("use_graph", ctypes.c_int32),
+    ]
+
+
 # Every exported symbol of include/fauxglcuda.h, with (restype, argtypes).
 _P = ctypes.c_void_p
 _PP = ctypes.POINTER(ctypes.c_void_p)
@@ -137,6 +163,17 @@ SIGNATURES = {
     "fgc_context_last_stats": (_I, [_P, ctypes.POINTER(FgcStats)]),
     "fgc_context_set_stream": (_I, [_P, _P]),
     "fgc_measure_fp64_rate": (_I, [_D]),
+    "fgc_batch_create": (_I, [_PP]),
+    "fgc_batch_destroy": (_I, [_P]),
+    "fgc_batch_set_stream": (_I, [_P, _P]),
+    "fgc_batch_set_tuning": (_I, [_P, ctypes.POINTER(FgcBatchTuning)]),
+    "fgc_batch_get_tuning": (_I, [_P, ctypes.POINTER(FgcBatchTuning)]),
+    "fgc_batch_set_timing": (_I, [_P, _I32]),
+    "fgc_batch_submit": (_I, [_P, ctypes.POINTER(FgcBatchItem), _U64]),
+    "fgc_batch_query": (_I, [_P, ctypes.POINTER(_I32)]),
+    "fgc_batch_wait": (_I, [_P, _INFO]),
+    "fgc_batch_last_stats": (_I, [_P, ctypes.POINTER(FgcStats)]),
+    "fgc_batch_autotune": (_I, [_P, ctypes.POINTER(FgcBatchItem), _U64, _I32, ctypes.POINTER(FgcBatchTuning)]),
 }
 
 _lib = None

@@ -1,88 +1,28 @@
 // fgc_api.cu -- host runtime of libfauxglcuda: the C ABI of
-// include/fauxglcuda.h, context / mesh / texture residency and the draw
-// pipeline orchestration.
+// include/fauxglcuda.h (contexts, meshes, textures, draws, read-back).
 //
-// A draw is one stream-ordered pipeline with a single host synchronisation
-// at its end (RasterizeInfo is returned by value, as DrawMesh returns it,
-// context.go:435-439):
-//   vertex_kernel            per unique position: Output, Outside, NDC, screen
-//   setup_triangles_kernel   culling, edge setup, ordered compaction
-//   setup_lines_kernel       lines after triangles (DrawMesh order)
-//   clip_*_kernel            ClipTriangle / ClipLine for flagged elements
-//   bin_count / scan / bin_scatter   stable band bins
-//   raster_kernel            fragments, shading, ordered resolve
-// Buffers grow on demand; when a kernel reports that a buffer was too small
-// (status word) the raster kernel leaves the framebuffer untouched and the
-// host re-runs the draw with the size the device measured.
-#include <cuda_runtime.h>
+// DrawMesh / DrawTriangles / DrawLines run a pass of one draw through the
+// pass engine (fgc_pass.cu) on the context's stream and wait for it: the
+// reference returns RasterizeInfo by value (context.go:391-439). The batch
+// interface (fgc_batch.cu) runs passes of many draws.
+#include "fgc_host.cuh"
 
-#include <algorithm>
-#include <cstring>
-#include <mutex>
 #include <new>
-#include <string>
-
-#include "fgc_internal.cuh"
 
 using namespace fgc;
 
-namespace {
+namespace fgc {
 
+namespace {
 thread_local std::string g_err = "";
+}  // namespace
 
 int fail(int code, const std::string& msg) {
     g_err = msg;
     return code;
 }
 
-#define FGC_CUDA(call)                                                                                        \
-    do {                                                                                                      \
-        cudaError_t e_ = (call);                                                                              \
-        if (e_ != cudaSuccess) return fail(FGC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
-    } while (0)
-
-template <typename T>
-struct DevBuf {
-    T* p = nullptr;
-    size_t cap = 0;
-    DevBuf() = default;
-    DevBuf(const DevBuf&) = delete;
-    DevBuf& operator=(const DevBuf&) = delete;
-    ~DevBuf() { release(); }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-    }
-    // Make room for n elements (contents not preserved when it grows).
-    cudaError_t ensure(size_t n) {
-        if (n <= cap && p) return cudaSuccess;
-        release();
-        size_t want = std::max<size_t>(n + n / 4, 64);
-        cudaError_t e = cudaMalloc((void**)&p, want * sizeof(T));
-        if (e != cudaSuccess) {
-            p = nullptr;
-            return e;
-        }
-        cap = want;
-        return cudaSuccess;
-    }
-};
-
-struct Counters {
-    unsigned int status;
-    unsigned int clip_count;
-    unsigned int lclip_count;
-    unsigned int band_counter;
-    unsigned int tick_tri, tick_line, tick_scan, pad;
-    unsigned long long tri_slots, line_slots, prim_total, pair_total;
-    unsigned long long info[4];  // total, updated, visited, shaded
-};
-
-constexpr int kRasterThreads = 256;
-constexpr int64_t kBandTarget = 4096;  // pixels per band (rounded to whole rows)
-constexpr int kFragCap = 1024;
-constexpr int kMaxBands = 24576;
+const char* last_error() { return g_err.c_str(); }
 
 int grid_for(uint64_t n, int block, int cap) {
     uint64_t g = (n + block - 1) / block;
@@ -102,116 +42,6 @@ uint32_t pack_nrgba_host(const double c[4]) {
         out |= (b & 0xff) << (8 * k);
     }
     return out;
-}
-
-}  // namespace
-
-struct fgc_texture {
-    int device = 0;
-    int32_t w = 0, h = 0;
-    DevBuf<ushort4> texels;
-};
-
-struct fgc_mesh {
-    int device = 0;
-    uint64_t ntri = 0, nline = 0, nuniq = 0;
-    DevBuf<double> ux, uy, uz;
-    DevBuf<uint32_t> corner_uniq;
-    DevBuf<APosNrm64> pn64;
-    DevBuf<APosNrm32> pn32;
-    DevBuf<double> tex64, col64;
-    DevBuf<float> tex32, col32;
-    bool has_tex = false, has_col = false;
-
-    MeshView view() const {
-        MeshView v;
-        v.ntri = ntri;
-        v.nline = nline;
-        v.nuniq = nuniq;
-        v.upos_x = ux.p;
-        v.upos_y = uy.p;
-        v.upos_z = uz.p;
-        v.corner_uniq = corner_uniq.p;
-        v.pn64 = pn64.p;
-        v.tex64 = has_tex ? tex64.p : nullptr;
-        v.col64 = has_col ? col64.p : nullptr;
-        v.pn32 = pn32.p;
-        v.tex32 = has_tex ? tex32.p : nullptr;
-        v.col32 = has_col ? col32.p : nullptr;
-        return v;
-    }
-};
-
-struct fgc_context {
-    int device = 0;
-    int sms = 1;
-    cudaStream_t stream = nullptr;      // the stream work is issued on
-    cudaStream_t own_stream = nullptr;  // the context's own stream
-    int32_t W = 0, H = 0;
-    int64_t N = 0;
-    DevBuf<uint32_t> color;
-    DevBuf<double> depth;
-    bool clear_color_pending = false, clear_depth_pending = false;
-    uint32_t clear_color = 0;
-    double clear_depth = 1.7976931348623157e308;
-    int debug = 0;
-    DevBuf<uint32_t> winner;
-    DevBuf<double> shaded, dbg;
-    // per-draw scratch
-    DevBuf<VClip> vclip;
-    DevBuf<double2> vndc;
-    DevBuf<VScreen> vscr;
-    DevBuf<uint8_t> vout;
-    DevBuf<RPrim> prims;
-    DevBuf<PBox> pbox;
-    DevBuf<uint32_t> pspan;
-    DevBuf<ulonglong2> clip_list, lclip_list;
-    DevBuf<PoolVertex> pool;
-    DevBuf<uint32_t> mat, off, bins;
-    DevBuf<unsigned long long> tiles;
-    DevBuf<Counters> counters;
-    DevBuf<unsigned long long> lohi;
-    DevBuf<uint32_t> ds;
-    DevBuf<uint16_t> gray;
-    Counters* host_counters = nullptr;
-    uint32_t clip_cap = 1024;
-    uint64_t bin_cap = 0;
-    bool timing = false;
-    cudaEvent_t ev[FGC_STAGE_COUNT + 1] = {};
-    fgc_stats stats = {};
-    std::mutex mu;
-};
-
-namespace {
-
-int apply_pending_clears(fgc_context* c) {
-    int grid = grid_for((uint64_t)c->N, 256, c->sms * 8);
-    if (c->clear_color_pending) {
-        fill_u32_kernel<<<grid, 256, 0, c->stream>>>(c->color.p, (uint64_t)c->N, c->clear_color);
-        FGC_CUDA(cudaGetLastError());
-        c->clear_color_pending = false;
-    }
-    if (c->clear_depth_pending) {
-        fill_f64_kernel<<<grid, 256, 0, c->stream>>>(c->depth.p, (uint64_t)c->N, c->clear_depth);
-        FGC_CUDA(cudaGetLastError());
-        c->clear_depth_pending = false;
-    }
-    return FGC_OK;
-}
-
-int ensure_debug(fgc_context* c) {
-    if (!(c->debug & (FGC_DEBUG_WINNER | FGC_DEBUG_SHADED_COLOR))) return FGC_OK;
-    int grid = grid_for((uint64_t)c->N, 256, c->sms * 8);
-    if ((c->debug & FGC_DEBUG_WINNER) && !c->winner.p) {
-        FGC_CUDA(c->winner.ensure((size_t)c->N));
-        fill_u32_kernel<<<grid, 256, 0, c->stream>>>(c->winner.p, (uint64_t)c->N, 0xFFFFFFFFu);
-        FGC_CUDA(cudaGetLastError());
-    }
-    if ((c->debug & FGC_DEBUG_SHADED_COLOR) && !c->shaded.p) {
-        FGC_CUDA(c->shaded.ensure((size_t)c->N * 4));
-        FGC_CUDA(cudaMemsetAsync(c->shaded.p, 0, (size_t)c->N * 4 * sizeof(double), c->stream));
-    }
-    return FGC_OK;
 }
 
 int fill_views(const fgc_state* st, const fgc_shader* sh, StateView& sv, ShaderView& shv) {
@@ -255,288 +85,42 @@ int fill_views(const fgc_state* st, const fgc_shader* sh, StateView& sv, ShaderV
     return FGC_OK;
 }
 
-struct DrawShape {
-    int32_t R;
-    int64_t L;
-    uint32_t nbands;
-    int F;
-    size_t smem;
-    int bin_warps;
-    uint32_t nblk;
-};
-
-int draw_shape(const fgc_context* c, DrawShape& s) {
-    int64_t R = std::max<int64_t>(1, kBandTarget / c->W);
-    R = std::min<int64_t>(R, kRasterThreads - 2);
-    R = std::min<int64_t>(R, c->H);
-    s.R = (int32_t)R;
-    s.L = R * c->W;
-    if (s.L > 65535) return fail(FGC_ERR_UNSUPPORTED, "frame width above 65535 pixels is not supported");
-    s.nbands = (uint32_t)((c->N + s.L - 1) / s.L);
-    if (s.nbands > (uint32_t)kMaxBands) return fail(FGC_ERR_UNSUPPORTED, "frame has too many bands");
-    s.F = kFragCap;
-    s.smem = raster_smem_bytes(s.L, s.F, kRasterThreads);
-    // two CTAs per SM (the register budget allows two) when a smaller
-    // fragment buffer makes them fit
-    while (s.smem > 112 * 1024 && s.F > 512) {
-        s.F -= 128;
-        s.smem = raster_smem_bytes(s.L, s.F, kRasterThreads);
+int ensure_debug(fgc_context* c) {
+    if (!(c->debug & (FGC_DEBUG_WINNER | FGC_DEBUG_SHADED_COLOR))) return FGC_OK;
+    int grid = grid_for((uint64_t)c->N, 256, c->sms * 8);
+    if ((c->debug & FGC_DEBUG_WINNER) && !c->winner.p) {
+        FGC_CUDA(c->winner.ensure((size_t)c->N));
+        fill_u32_kernel<<<grid, 256, 0, c->stream>>>(c->winner.p, (uint64_t)c->N, 0xFFFFFFFFu);
+        FGC_CUDA(cudaGetLastError());
     }
-    while (s.smem > 227 * 1024 && s.F > 256) {
-        s.F /= 2;
-        s.smem = raster_smem_bytes(s.L, s.F, kRasterThreads);
+    if ((c->debug & FGC_DEBUG_SHADED_COLOR) && !c->shaded.p) {
+        FGC_CUDA(c->shaded.ensure((size_t)c->N * 4));
+        FGC_CUDA(cudaMemsetAsync(c->shaded.p, 0, (size_t)c->N * 4 * sizeof(double), c->stream));
     }
-    if (s.smem > 227 * 1024) return fail(FGC_ERR_UNSUPPORTED, "frame too wide for the band rasteriser");
-    int warps = (int)std::min<int64_t>(8, (96 * 1024) / ((int64_t)s.nbands * 4));
-    if (warps < 1) return fail(FGC_ERR_UNSUPPORTED, "frame has too many bands for binning");
-    s.bin_warps = warps;
-    s.nblk = (uint32_t)(2 * c->sms);
     return FGC_OK;
 }
 
-void mark(fgc_context* c, int i) {
-    if (c->timing) cudaEventRecord(c->ev[i], c->stream);
+int context_ready(const fgc_context* c) {
+    if (c->busy) return fail(FGC_ERR_BUSY, "the context has draws in an unfinished batch");
+    return FGC_OK;
 }
 
-int run_draw(fgc_context* c, const fgc_mesh* m, uint64_t tf, uint64_t tc, uint64_t lf, uint64_t lc,
-             const StateView& sv, const ShaderView& shv, bool* retry) {
-    *retry = false;
-    uint64_t launches = 0;
-    DrawShape shape;
-    int rc = draw_shape(c, shape);
-    if (rc) return rc;
-    const int per = sv.wireframe ? 6 : 1;
-    const uint64_t prim_cap = tc * per + (uint64_t)c->clip_cap * (uint64_t)(7 * per - per) + lc * 2 + 1;
-    const uint64_t tri_tiles = (tc + 255) / 256, line_tiles = (lc + 255) / 256;
-    const uint64_t nmat = (uint64_t)shape.nbands * shape.nblk;
-    const uint64_t scan_tiles = (nmat + 2047) / 2048;
-    if (c->bin_cap == 0) c->bin_cap = std::max<uint64_t>(2 * prim_cap, 1 << 16);
+}  // namespace fgc
 
-    FGC_CUDA(c->vclip.ensure(m->nuniq + 1));
-    FGC_CUDA(c->vndc.ensure(m->nuniq + 1));
-    FGC_CUDA(c->vscr.ensure(m->nuniq + 1));
-    FGC_CUDA(c->vout.ensure(m->nuniq + 1));
-    FGC_CUDA(c->prims.ensure(prim_cap));
-    FGC_CUDA(c->pbox.ensure(prim_cap));
-    FGC_CUDA(c->pspan.ensure(prim_cap));
-    FGC_CUDA(c->clip_list.ensure(c->clip_cap));
-    FGC_CUDA(c->pool.ensure((size_t)c->clip_cap * 21));
-    FGC_CUDA(c->lclip_list.ensure(lc + 1));
-    FGC_CUDA(c->mat.ensure(nmat));
-    FGC_CUDA(c->off.ensure(nmat));
-    FGC_CUDA(c->bins.ensure(c->bin_cap));
-    FGC_CUDA(c->tiles.ensure(tri_tiles + line_tiles + scan_tiles + 3));
-    FGC_CUDA(c->counters.ensure(1));
-    if (!c->host_counters) FGC_CUDA(cudaMallocHost((void**)&c->host_counters, sizeof(Counters)));
-    rc = ensure_debug(c);
-    if (rc) return rc;
+namespace {
 
-    FGC_CUDA(cudaMemsetAsync(c->counters.p, 0, sizeof(Counters), c->stream));
-    FGC_CUDA(cudaMemsetAsync(c->tiles.p, 0, (tri_tiles + line_tiles + scan_tiles + 3) * 8, c->stream));
-    Counters* dc = c->counters.p;
-    unsigned long long* t_tri = c->tiles.p;
-    unsigned long long* t_line = t_tri + tri_tiles + 1;
-    unsigned long long* t_scan = t_line + line_tiles + 1;
-
-    const double w2 = (double)c->W / 2, h2 = (double)c->H / 2;
-    mark(c, 0);
-    if (m->nuniq > 0 && (tc > 0 || lc > 0)) {
-        VertexParams vp;
-        vp.ux = m->ux.p;
-        vp.uy = m->uy.p;
-        vp.uz = m->uz.p;
-        vp.n = m->nuniq;
-        memcpy(vp.m, shv.m, sizeof(vp.m));
-        vp.w2 = w2;
-        vp.h2 = h2;
-        vp.vclip = c->vclip.p;
-        vp.vndc = c->vndc.p;
-        vp.vscr = c->vscr.p;
-        vp.vout = c->vout.p;
-        vertex_kernel<<<grid_for(m->nuniq, 256, c->sms * 16), 256, 0, c->stream>>>(vp);
+int apply_pending_clears(fgc_context* c) {
+    int grid = grid_for((uint64_t)c->N, 256, c->sms * 8);
+    if (c->clear_color_pending) {
+        fill_u32_kernel<<<grid, 256, 0, c->stream>>>(c->color.p, (uint64_t)c->N, c->clear_color);
         FGC_CUDA(cudaGetLastError());
-        launches++;
+        c->clear_color_pending = false;
     }
-    mark(c, 1);
-
-    GeomParams gp;
-    memset(&gp, 0, sizeof(gp));
-    gp.mesh = m->view();
-    gp.st = sv;
-    gp.w2 = w2;
-    gp.h2 = h2;
-    gp.tri_first = tf;
-    gp.tri_count = tc;
-    gp.line_first = lf;
-    gp.line_count = lc;
-    gp.vclip = c->vclip.p;
-    gp.vndc = c->vndc.p;
-    gp.vscr = c->vscr.p;
-    gp.vout = c->vout.p;
-    gp.prims = c->prims.p;
-    gp.pbox = c->pbox.p;
-    gp.pspan = c->pspan.p;
-    gp.prim_cap = prim_cap;
-    gp.clip_list = c->clip_list.p;
-    gp.clip_cap = c->clip_cap;
-    gp.clip_count = &dc->clip_count;
-    gp.lclip_list = c->lclip_list.p;
-    gp.lclip_count = &dc->lclip_count;
-    gp.pool = c->pool.p;
-    gp.attr_mask = 0;
-    if (shv.kind == FGC_SHADER_PHONG) {
-        gp.attr_mask |= kAttrPos | kAttrNrm;
-        if (shv.object_is_discard) gp.attr_mask |= kAttrCol;
-    }
-    if (shv.has_texture || shv.kind == FGC_SHADER_TEXTURE) gp.attr_mask |= kAttrTex;
-    gp.tri_slots = &dc->tri_slots;
-    gp.line_slots = &dc->line_slots;
-    gp.prim_total = &dc->prim_total;
-    gp.lb_tri = Lookback{t_tri, &dc->tick_tri, &dc->status, &dc->tri_slots};
-    gp.lb_line = Lookback{t_line, &dc->tick_line, &dc->status, &dc->line_slots};
-    gp.status = &dc->status;
-    if (tc > 0) {
-        setup_triangles_kernel<<<(unsigned)tri_tiles, 256, 0, c->stream>>>(gp);
+    if (c->clear_depth_pending) {
+        fill_f64_kernel<<<grid, 256, 0, c->stream>>>(c->depth.p, (uint64_t)c->N, c->clear_depth);
         FGC_CUDA(cudaGetLastError());
-        launches++;
+        c->clear_depth_pending = false;
     }
-    if (lc > 0) {
-        setup_lines_kernel<<<(unsigned)line_tiles, 256, 0, c->stream>>>(gp);
-        FGC_CUDA(cudaGetLastError());
-        launches++;
-    }
-    mark(c, 2);
-    if (tc > 0) {
-        clip_triangles_kernel<<<grid_for(c->clip_cap, 128, c->sms * 4), 128, 0, c->stream>>>(gp);
-        FGC_CUDA(cudaGetLastError());
-        launches++;
-    }
-    if (lc > 0) {
-        clip_lines_kernel<<<grid_for(lc, 128, c->sms * 4), 128, 0, c->stream>>>(gp);
-        FGC_CUDA(cudaGetLastError());
-        launches++;
-    }
-    prim_total_kernel<<<1, 1, 0, c->stream>>>(gp);
-    FGC_CUDA(cudaGetLastError());
-    launches++;
-    mark(c, 3);
-
-    BinParams bp;
-    bp.pbox = c->pbox.p;
-    bp.nprim = &dc->prim_total;
-    bp.W = c->W;
-    bp.N = c->N;
-    bp.L = shape.L;
-    bp.nbands = shape.nbands;
-    bp.nblk = shape.nblk;
-    bp.mat = c->mat.p;
-    bp.off = c->off.p;
-    bp.pair_total = &dc->pair_total;
-    bp.bins = c->bins.p;
-    bp.bin_cap = c->bin_cap;
-    bp.status = &dc->status;
-    size_t hist_smem = (size_t)shape.nbands * 4;
-    if (hist_smem > 48 * 1024)
-        FGC_CUDA(cudaFuncSetAttribute(bin_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem));
-    bin_count_kernel<<<shape.nblk, 256, hist_smem, c->stream>>>(bp);
-    FGC_CUDA(cudaGetLastError());
-    ScanParams sp;
-    sp.in = c->mat.p;
-    sp.out = c->off.p;
-    sp.n = nmat;
-    sp.lb = Lookback{t_scan, &dc->tick_scan, &dc->status, &dc->pair_total};
-    scan_u32_kernel<<<(unsigned)scan_tiles, 256, 0, c->stream>>>(sp);
-    FGC_CUDA(cudaGetLastError());
-    size_t scat_smem = (size_t)shape.bin_warps * shape.nbands * 4;
-    if (scat_smem > 48 * 1024)
-        FGC_CUDA(cudaFuncSetAttribute(bin_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scat_smem));
-    bin_scatter_kernel<<<shape.nblk, shape.bin_warps * 32, scat_smem, c->stream>>>(bp, shape.bin_warps);
-    FGC_CUDA(cudaGetLastError());
-    launches += 3;
-    mark(c, 4);
-
-    RasterParams rp;
-    memset(&rp, 0, sizeof(rp));
-    rp.prims = c->prims.p;
-    rp.pbox = c->pbox.p;
-    rp.pspan = c->pspan.p;
-    rp.bins = c->bins.p;
-    rp.off = c->off.p;
-    rp.pair_total = &dc->pair_total;
-    rp.nblk = shape.nblk;
-    rp.nbands = shape.nbands;
-    rp.W = c->W;
-    rp.H = c->H;
-    rp.N = c->N;
-    rp.L = shape.L;
-    rp.F = shape.F;
-    rp.color = c->color.p;
-    rp.depth = c->depth.p;
-    rp.clear_color_pending = c->clear_color_pending;
-    rp.clear_depth_pending = c->clear_depth_pending;
-    rp.clear_color = c->clear_color;
-    rp.clear_depth = c->clear_depth;
-    rp.st = sv;
-    rp.sh = shv;
-    rp.mesh = m->view();
-    rp.pool = c->pool.p;
-    rp.band_counter = &dc->band_counter;
-    rp.status = &dc->status;
-    rp.info = dc->info;
-    const void* kfn = raster_kernel_ptr(sv.precision);
-    FGC_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shape.smem));
-    int per_sm = 0;
-    FGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kRasterThreads, shape.smem));
-    if (per_sm < 1) return fail(FGC_ERR_UNSUPPORTED, "raster kernel does not fit on an SM");
-    int rgrid = (int)std::min<uint64_t>((uint64_t)per_sm * c->sms, shape.nbands);
-    if (c->debug & FGC_DEBUG_WINNER) rp.winner = c->winner.p;
-    if (c->debug & FGC_DEBUG_SHADED_COLOR) {
-        FGC_CUDA(c->dbg.ensure((size_t)rgrid * shape.F * 4));
-        rp.shaded = c->shaded.p;
-        rp.dbg = c->dbg.p;
-    }
-    FGC_CUDA(launch_raster(sv.precision, rgrid, kRasterThreads, shape.smem, c->stream, rp));
-    launches++;
-    mark(c, 5);
-
-    FGC_CUDA(cudaMemcpyAsync(c->host_counters, c->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream));
-    FGC_CUDA(cudaStreamSynchronize(c->stream));
-    const Counters& hc = *c->host_counters;
-    fgc_stats& S = c->stats;
-    S.kernel_launches += launches;
-    S.attempts++;
-    S.elements = tc + lc;
-    S.unique_vertices = (tc > 0 || lc > 0) ? m->nuniq : 0;
-    S.clipped = (uint64_t)hc.clip_count + hc.lclip_count;
-    S.primitives = hc.prim_total;
-    S.bin_entries = hc.pair_total;
-    S.covered_pixels = hc.info[0];
-    S.updated_pixels = hc.info[1];
-    S.visited_pixels = hc.info[2];
-    S.shaded_fragments = hc.info[3];
-    S.bands = shape.nbands;
-    S.band_rows = (uint32_t)shape.R;
-    for (int i = 0; i < FGC_STAGE_COUNT; i++) {
-        float ms = 0;
-        if (c->timing) cudaEventElapsedTime(&ms, c->ev[i], c->ev[i + 1]);
-        S.stage_ms[i] = ms;
-    }
-    if (hc.status & ST_RASTER_INTERNAL)
-        return fail(FGC_ERR_DEVICE_LIMIT, "the raster stage detected an internal inconsistency");
-    if (hc.status & ST_LOOKBACK_TIMEOUT)
-        return fail(FGC_ERR_DEVICE_LIMIT, "a look-back wait in the setup or scan stage timed out");
-    if (hc.status & (ST_CLIP_OVERFLOW | ST_POOL_OVERFLOW)) {
-        c->clip_cap = std::max<uint32_t>(c->clip_cap * 2, hc.clip_count + hc.clip_count / 4 + 64);
-        *retry = true;
-        return FGC_OK;
-    }
-    if (hc.status & ST_BIN_OVERFLOW) {
-        c->bin_cap = hc.pair_total + hc.pair_total / 4 + 1024;
-        *retry = true;
-        return FGC_OK;
-    }
-    c->clear_color_pending = false;
-    c->clear_depth_pending = false;
     return FGC_OK;
 }
 
@@ -548,26 +132,42 @@ int draw(fgc_context* c, const fgc_mesh* m, uint64_t tf, uint64_t tc, uint64_t l
     if (lf > m->nline || lc > m->nline - lf) return fail(FGC_ERR_INVALID_ARGUMENT, "line range out of bounds");
     if (sh->texture && sh->texture->device != c->device)
         return fail(FGC_ERR_INVALID_ARGUMENT, "texture is on another device");
-    StateView sv;
-    ShaderView shv;
-    int rc = fill_views(st, sh, sv, shv);
+    Submission sub;
+    sub.items.resize(1);
+    PassItem& it = sub.items[0];
+    int rc = fill_views(st, sh, it.sv, it.shv);
     if (rc) return rc;
     std::lock_guard<std::mutex> lock(c->mu);
+    rc = context_ready(c);
+    if (rc) return rc;
     FGC_CUDA(cudaSetDevice(c->device));
-    c->stats = fgc_stats{};
-    for (int attempt = 0; attempt < 8; attempt++) {
-        bool retry = false;
-        rc = run_draw(c, m, tf, tc, lf, lc, sv, shv, &retry);
-        if (rc) return rc;
-        if (!retry) {
-            if (info) {
-                info->total_pixels = c->host_counters->info[0];
-                info->updated_pixels = c->host_counters->info[1];
-            }
-            return FGC_OK;
-        }
-    }
-    return fail(FGC_ERR_DEVICE_LIMIT, "draw buffers kept overflowing");
+    const DevLimits* D = nullptr;
+    rc = dev_limits(c->device, &D);
+    if (rc) return rc;
+    rc = ensure_debug(c);
+    if (rc) return rc;
+    it.ctx = c;
+    it.mesh = m;
+    it.tf = tf;
+    it.tc = tc;
+    it.lf = lf;
+    it.lc = lc;
+    it.clear_color = c->clear_color_pending;
+    it.clear_depth = c->clear_depth_pending;
+    it.clear_color_value = c->clear_color;
+    it.clear_depth_value = c->clear_depth;
+    sub.timing = c->timing;
+    static const PassTuning kDefaultTuning;
+    rc = run_submission(c->scratch, c->stream, *D, kDefaultTuning, sub);
+    c->stats = sub.stats;
+    c->stats.elements = tc + lc;
+    c->stats.unique_vertices = (tc > 0 || lc > 0) ? m->nuniq : 0;
+    if (rc) return rc;
+    // the pass applied the pending clears (fused into its raster stage)
+    c->clear_color_pending = false;
+    c->clear_depth_pending = false;
+    if (info) *info = sub.infos[0];
+    return FGC_OK;
 }
 
 }  // namespace
@@ -579,7 +179,7 @@ extern "C" {
 
 int32_t fgc_abi_version(void) { return FGC_ABI_VERSION; }
 
-const char* fgc_last_error(void) { return g_err.c_str(); }
+const char* fgc_last_error(void) { return fgc::last_error(); }
 
 void fgc_state_default(fgc_state* st) {
     if (!st) return;
@@ -631,6 +231,7 @@ int fgc_context_create(int32_t width, int32_t height, fgc_context** out) {
     *out = nullptr;
     if (width < 1 || height < 1) return fail(FGC_ERR_INVALID_ARGUMENT, "width and height must be positive");
     if ((int64_t)width * height > (int64_t)1 << 34) return fail(FGC_ERR_INVALID_ARGUMENT, "frame too large");
+    if (height > (1 << 30)) return fail(FGC_ERR_UNSUPPORTED, "frame height above 2^30 rows is not supported");
     fgc_context* c = new (std::nothrow) fgc_context();
     if (!c) return fail(FGC_ERR_OUT_OF_MEMORY, "host allocation failed");
     auto bail = [&](int rc) {
@@ -643,10 +244,6 @@ int fgc_context_create(int32_t width, int32_t height, fgc_context** out) {
     e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return bail(fail(FGC_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)));
     c->stream = c->own_stream;
-    for (int i = 0; i <= FGC_STAGE_COUNT; i++) {
-        e = cudaEventCreate(&c->ev[i]);
-        if (e != cudaSuccess) return bail(fail(FGC_ERR_CUDA, std::string("cudaEventCreate: ") + cudaGetErrorString(e)));
-    }
     c->W = width;
     c->H = height;
     c->N = (int64_t)width * height;
@@ -664,11 +261,13 @@ int fgc_context_create(int32_t width, int32_t height, fgc_context** out) {
 
 int fgc_context_destroy(fgc_context* c) {
     if (!c) return FGC_OK;
+    {
+        std::lock_guard<std::mutex> lock(c->mu);
+        int rc = context_ready(c);
+        if (rc) return rc;
+    }
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
-    if (c->host_counters) cudaFreeHost(c->host_counters);
-    for (int i = 0; i <= FGC_STAGE_COUNT; i++)
-        if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
     return FGC_OK;
@@ -684,6 +283,7 @@ int fgc_context_size(const fgc_context* c, int32_t* w, int32_t* h) {
 int fgc_context_set_debug(fgc_context* c, int32_t flags) {
     if (!c) return fail(FGC_ERR_INVALID_ARGUMENT, "null context");
     std::lock_guard<std::mutex> lock(c->mu);
+    if (int rc_ = context_ready(c)) return rc_;
     FGC_CUDA(cudaSetDevice(c->device));
     c->debug = flags;
     int rc = ensure_debug(c);
@@ -695,6 +295,7 @@ int fgc_context_set_debug(fgc_context* c, int32_t flags) {
 int fgc_context_set_timing(fgc_context* c, int32_t enable) {
     if (!c) return fail(FGC_ERR_INVALID_ARGUMENT, "null context");
     std::lock_guard<std::mutex> lock(c->mu);
+    if (int rc_ = context_ready(c)) return rc_;
     c->timing = enable != 0;
     return FGC_OK;
 }
@@ -708,6 +309,7 @@ int fgc_context_last_stats(const fgc_context* c, fgc_stats* out) {
 int fgc_context_set_stream(fgc_context* c, void* cuda_stream) {
     if (!c) return fail(FGC_ERR_INVALID_ARGUMENT, "null context");
     std::lock_guard<std::mutex> lock(c->mu);
+    if (int rc_ = context_ready(c)) return rc_;
     FGC_CUDA(cudaSetDevice(c->device));
     FGC_CUDA(cudaStreamSynchronize(c->stream));
     c->stream = cuda_stream ? (cudaStream_t)cuda_stream : c->own_stream;
@@ -753,6 +355,7 @@ int fgc_measure_fp64_rate(double* gops_per_s) {
 int fgc_clear_color(fgc_context* c, const double rgba[4]) {
     if (!c || !rgba) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
     std::lock_guard<std::mutex> lock(c->mu);
+    if (int rc_ = context_ready(c)) return rc_;
     c->clear_color = pack_nrgba_host(rgba);
     c->clear_color_pending = true;
     return FGC_OK;
@@ -761,6 +364,7 @@ int fgc_clear_color(fgc_context* c, const double rgba[4]) {
 int fgc_clear_depth(fgc_context* c, double value) {
     if (!c) return fail(FGC_ERR_INVALID_ARGUMENT, "null context");
     std::lock_guard<std::mutex> lock(c->mu);
+    if (int rc_ = context_ready(c)) return rc_;
     c->clear_depth = value;
     c->clear_depth_pending = true;
     return FGC_OK;
@@ -946,6 +550,7 @@ int fgc_draw_lines(fgc_context* c, const fgc_mesh* m, uint64_t first, uint64_t c
 int fgc_read_color(fgc_context* c, uint8_t* nrgba) {
     if (!c || !nrgba) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
     std::lock_guard<std::mutex> lock(c->mu);
+    if (int rc_ = context_ready(c)) return rc_;
     FGC_CUDA(cudaSetDevice(c->device));
     int rc = apply_pending_clears(c);
     if (rc) return rc;
@@ -957,6 +562,7 @@ int fgc_read_color(fgc_context* c, uint8_t* nrgba) {
 int fgc_read_depth(fgc_context* c, double* depth) {
     if (!c || !depth) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
     std::lock_guard<std::mutex> lock(c->mu);
+    if (int rc_ = context_ready(c)) return rc_;
     FGC_CUDA(cudaSetDevice(c->device));
     int rc = apply_pending_clears(c);
     if (rc) return rc;
@@ -968,6 +574,7 @@ int fgc_read_depth(fgc_context* c, double* depth) {
 int fgc_write_color(fgc_context* c, const uint8_t* nrgba) {
     if (!c || !nrgba) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
     std::lock_guard<std::mutex> lock(c->mu);
+    if (int rc_ = context_ready(c)) return rc_;
     FGC_CUDA(cudaSetDevice(c->device));
     c->clear_color_pending = false;
     FGC_CUDA(cudaMemcpyAsync(c->color.p, nrgba, (size_t)c->N * 4, cudaMemcpyHostToDevice, c->stream));
@@ -978,6 +585,7 @@ int fgc_write_color(fgc_context* c, const uint8_t* nrgba) {
 int fgc_write_depth(fgc_context* c, const double* depth) {
     if (!c || !depth) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
     std::lock_guard<std::mutex> lock(c->mu);
+    if (int rc_ = context_ready(c)) return rc_;
     FGC_CUDA(cudaSetDevice(c->device));
     c->clear_depth_pending = false;
     FGC_CUDA(cudaMemcpyAsync(c->depth.p, depth, (size_t)c->N * 8, cudaMemcpyHostToDevice, c->stream));
@@ -988,6 +596,7 @@ int fgc_write_depth(fgc_context* c, const double* depth) {
 int fgc_depth_image(fgc_context* c, uint16_t* gray16) {
     if (!c || !gray16) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
     std::lock_guard<std::mutex> lock(c->mu);
+    if (int rc_ = context_ready(c)) return rc_;
     FGC_CUDA(cudaSetDevice(c->device));
     int rc = apply_pending_clears(c);
     if (rc) return rc;
@@ -1010,6 +619,7 @@ int fgc_downsample(fgc_context* c, int32_t scale, uint8_t* out) {
     if (scale < 1 || c->W % scale != 0 || c->H % scale != 0)
         return fail(FGC_ERR_INVALID_ARGUMENT, "scale must divide width and height");
     std::lock_guard<std::mutex> lock(c->mu);
+    if (int rc_ = context_ready(c)) return rc_;
     FGC_CUDA(cudaSetDevice(c->device));
     int rc = apply_pending_clears(c);
     if (rc) return rc;
@@ -1026,6 +636,7 @@ int fgc_read_winner(fgc_context* c, uint32_t* winner) {
     if (!c || !winner) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
     if (!(c->debug & FGC_DEBUG_WINNER) || !c->winner.p) return fail(FGC_ERR_INVALID_ARGUMENT, "winner ids are off");
     std::lock_guard<std::mutex> lock(c->mu);
+    if (int rc_ = context_ready(c)) return rc_;
     FGC_CUDA(cudaSetDevice(c->device));
     FGC_CUDA(cudaMemcpyAsync(winner, c->winner.p, (size_t)c->N * 4, cudaMemcpyDeviceToHost, c->stream));
     FGC_CUDA(cudaStreamSynchronize(c->stream));
@@ -1037,6 +648,7 @@ int fgc_read_shaded_color(fgc_context* c, double* rgba) {
     if (!(c->debug & FGC_DEBUG_SHADED_COLOR) || !c->shaded.p)
         return fail(FGC_ERR_INVALID_ARGUMENT, "shaded colours are off");
     std::lock_guard<std::mutex> lock(c->mu);
+    if (int rc_ = context_ready(c)) return rc_;
     FGC_CUDA(cudaSetDevice(c->device));
     FGC_CUDA(cudaMemcpyAsync(rgba, c->shaded.p, (size_t)c->N * 32, cudaMemcpyDeviceToHost, c->stream));
     FGC_CUDA(cudaStreamSynchronize(c->stream));
@@ -1098,6 +710,7 @@ extern "C" int fgc_depth_image_noalloc(fgc_context* c, uint16_t* gray16) {
                     "fgc_depth_image_noalloc handles at most 8388608 pixels (its static scratch is 16 MiB); "
                     "use fgc_depth_image for larger frames");
     std::lock_guard<std::mutex> lock(c->mu);
+    if (int rc_ = context_ready(c)) return rc_;
     FGC_CUDA(cudaSetDevice(c->device));
     unsigned char* base = nullptr;
     int rc = noalloc_scratch(c->device, &base);

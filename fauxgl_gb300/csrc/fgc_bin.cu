@@ -9,9 +9,11 @@
 //
 // The bins must list primitives in submission order (ties resolve "later
 // wins", context.go:248). Count, scan and scatter are all integer and
-// deterministic:
-//   bin_count    per-block band histograms -> mat[band][block]
-//   scan_u32     exclusive scan of mat in (band, block) order -> off
+// deterministic. Every draw of a pass owns a run of binning blocks, a
+// [band][block] slab of the count matrix and a run of bands:
+//   bin_count    per-block band histograms -> mat[draw][band][block]
+//   scan_u32     one exclusive scan of the whole matrix -> off (a draw's
+//                bins follow the previous draw's)
 //   bin_scatter  per block, warps own consecutive sub-ranges; a stable rank
 //                inside each 32-primitive round comes from comparing band
 //                ranges across lanes, so the output order is the input order.
@@ -19,36 +21,68 @@
 
 namespace fgc {
 
-__device__ __forceinline__ bool prim_bands(const BinParams& P, const PBox& b, uint32_t& bl, uint32_t& bh) {
+// The draw's band geometry, as the binning blocks use it.
+struct BandGeom {
+    int32_t W, H, R;
+    uint32_t nbands;
+};
+
+// Bands [bl, bh] that the box's linear index range [y0*W + x0, y1*W + x1],
+// clipped to [0, W*H), meets. Index y*W + x lies in row y + floor(x/W), and
+// band b holds rows [b*R, b*R + R).
+__device__ __forceinline__ bool prim_bands(const BandGeom& G, const PBox& b, uint32_t& bl, uint32_t& bh) {
     if (b.x0 > b.x1) return false;
-    int64_t lo = (int64_t)b.y0 * P.W + b.x0;
-    int64_t hi = (int64_t)b.y1 * P.W + b.x1;
-    if (lo < 0) lo = 0;
-    if (hi > P.N - 1) hi = P.N - 1;
-    if (lo > hi) return false;
-    bl = (uint32_t)(lo / P.L);
-    bh = (uint32_t)(hi / P.L);
+    int64_t rlo = (int64_t)b.y0 + floordiv_w(b.x0, G.W);
+    int64_t rhi = (int64_t)b.y1 + floordiv_w(b.x1, G.W);
+    if (rhi < 0 || rlo > G.H - 1) return false;
+    if (rlo < 0) rlo = 0;
+    if (rhi > G.H - 1) rhi = G.H - 1;
+    bl = (uint32_t)rlo / (uint32_t)G.R;
+    bh = (uint32_t)rhi / (uint32_t)G.R;
     return true;
 }
 
 constexpr unsigned int kRetryBits = ST_CLIP_OVERFLOW | ST_POOL_OVERFLOW | ST_LOOKBACK_TIMEOUT;
 
+// A binning block's draw and its share [lo, hi) of the draw's primitives.
+struct BinBlock {
+    uint32_t item, lblk, nblk;
+    uint64_t mat0;
+    uint64_t lo, hi;
+    BandGeom G;
+};
+
+__device__ __forceinline__ BinBlock bin_block(const BinParams& P) {
+    BinBlock B;
+    B.item = find_item(P.starts.blk, P.nitems, blockIdx.x);
+    const ItemView& I = P.items[B.item];
+    B.lblk = blockIdx.x - I.blk0;
+    B.nblk = I.nblk;
+    B.mat0 = I.mat0;
+    B.G = BandGeom{I.W, I.H, I.R, I.nbands};
+    // a failed earlier stage means this pass is re-run: bin nothing
+    const bool skip = (*P.status & kRetryBits) != 0;
+    const uint64_t p0 = P.iout[B.item].prim_start;
+    const uint64_t n = skip ? 0 : P.iout[B.item].prim_end - p0;
+    const uint64_t chunk = (n + B.nblk - 1) / B.nblk;
+    B.lo = p0 + min((uint64_t)B.lblk * chunk, n);
+    B.hi = p0 + min((uint64_t)B.lblk * chunk + chunk, n);
+    return B;
+}
+
 __global__ void __launch_bounds__(256) bin_count_kernel(BinParams P) {
     extern __shared__ uint32_t hist[];
-    // a failed earlier stage means this draw is re-run: count nothing
-    const uint64_t n = (*P.status & kRetryBits) ? 0 : *P.nprim;
-    const uint64_t chunk = (n + P.nblk - 1) / P.nblk;
-    const uint64_t lo = blockIdx.x * chunk;
-    const uint64_t hi = min(lo + chunk, n);
-    for (uint32_t i = threadIdx.x; i < P.nbands; i += blockDim.x) hist[i] = 0;
+    const BinBlock B = bin_block(P);
+    const uint32_t nb = B.G.nbands;
+    for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) hist[i] = 0;
     __syncthreads();
-    for (uint64_t p = lo + threadIdx.x; p < hi; p += blockDim.x) {
+    for (uint64_t p = B.lo + threadIdx.x; p < B.hi; p += blockDim.x) {
         uint32_t bl, bh;
-        if (prim_bands(P, P.pbox[p], bl, bh))
+        if (prim_bands(B.G, P.pbox[p], bl, bh))
             for (uint32_t b = bl; b <= bh; b++) atomicAdd(&hist[b], 1u);
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < P.nbands; i += blockDim.x) P.mat[(uint64_t)i * P.nblk + blockIdx.x] = hist[i];
+    for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) P.mat[B.mat0 + (uint64_t)i * B.nblk + B.lblk] = hist[i];
 }
 
 // Exclusive scan of n uint32 values, 2048 per logical block, single pass.
@@ -81,13 +115,11 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(BinParams P, int warps
         if (threadIdx.x == 0) atomicOr(P.status, ST_BIN_OVERFLOW);
         return;
     }
-    const uint32_t nb = P.nbands;
-    const uint64_t n = (*P.status & kRetryBits) ? 0 : *P.nprim;
-    const uint64_t chunk = (n + P.nblk - 1) / P.nblk;
-    const uint64_t lo = blockIdx.x * chunk;
-    const uint64_t hi = min(lo + chunk, n);
+    const BinBlock B = bin_block(P);
+    const uint32_t nb = B.G.nbands;
+    const uint64_t lo = B.lo, hi = B.hi;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint64_t sub = (chunk + warps - 1) / warps;
+    const uint64_t sub = (hi - lo + warps - 1) / warps;
     const uint64_t slo = min(lo + (uint64_t)w * sub, hi);
     const uint64_t shi = min(slo + sub, hi);
     uint32_t* mycnt = cnt + (size_t)w * nb;
@@ -97,13 +129,13 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(BinParams P, int warps
     // phase 1: per-warp band counts
     for (uint64_t p = slo + lane; p < shi; p += 32) {
         uint32_t bl, bh;
-        if (prim_bands(P, P.pbox[p], bl, bh))
+        if (prim_bands(B.G, P.pbox[p], bl, bh))
             for (uint32_t b = bl; b <= bh; b++) atomicAdd(&mycnt[b], 1u);
     }
     __syncthreads();
     // phase 2: each warp's starting position per band
     for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) {
-        uint32_t run = P.off[(uint64_t)b * P.nblk + blockIdx.x];
+        uint32_t run = P.off[B.mat0 + (uint64_t)b * B.nblk + B.lblk];
         for (int ww = 0; ww < warps; ww++) {
             uint32_t t = cnt[(size_t)ww * nb + b];
             cnt[(size_t)ww * nb + b] = run;
@@ -121,7 +153,7 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(BinParams P, int warps
     for (uint64_t rb = slo; rb < shi; rb += 32) {
         const uint64_t p = rb + lane;
         uint32_t bl = 1, bh = 0;
-        bool has = (p < shi) && prim_bands(P, P.pbox[p], bl, bh);
+        bool has = (p < shi) && prim_bands(B.G, P.pbox[p], bl, bh);
         const uint32_t span = has ? (bh - bl + 1) : 0u;
         uint32_t incl = span;
 #pragma unroll

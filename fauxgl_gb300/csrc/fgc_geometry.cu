@@ -15,17 +15,24 @@
 namespace fgc {
 
 // ---------------------------------------------------------------------------
-// Vertex stage: one thread per unique position.
+// Vertex stage: one thread per unique position of each draw (a draw's
+// positions are transformed by its own matrix), tiles of kVertexTile
+// positions strided over the grid.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) vertex_kernel(VertexParams P) {
-    for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < P.n; u += (uint64_t)gridDim.x * blockDim.x) {
-        D4 c = mul_position_w(P.m, P.ux[u], P.uy[u], P.uz[u]);  // Shader.Vertex
-        P.vclip[u] = VClip{c.x, c.y, c.z, c.w};
-        P.vout[u] = outside4(c) ? 1 : 0;
+__global__ void __launch_bounds__(kVertexTile) vertex_kernel(VertexParams P) {
+    for (uint32_t t = blockIdx.x; t < P.ntiles; t += gridDim.x) {
+        const uint32_t it = find_item(P.starts.vtile, P.nitems, t);
+        const ItemView& I = P.items[it];
+        const uint64_t u = (uint64_t)(t - I.vtile0) * kVertexTile + threadIdx.x;
+        if (u >= I.mesh.nuniq) continue;
+        D4 c = mul_position_w(I.sh.m, I.mesh.upos_x[u], I.mesh.upos_y[u], I.mesh.upos_z[u]);  // Shader.Vertex
+        const uint64_t o = I.vbase + u;
+        P.vclip[o] = VClip{c.x, c.y, c.z, c.w};
+        P.vout[o] = outside4(c) ? 1 : 0;
         D3 n = ndc_of(c);
-        P.vndc[u] = make_double2(n.x, n.y);
-        D3 s = screen_of_ndc(n, P.w2, P.h2);
-        P.vscr[u] = VScreen{s.x, s.y, s.z, __drcp_rn(c.w)};
+        P.vndc[o] = make_double2(n.x, n.y);
+        D3 s = screen_of_ndc(n, I.w2, I.h2);
+        P.vscr[o] = VScreen{s.x, s.y, s.z, __drcp_rn(c.w)};
     }
 }
 
@@ -111,9 +118,9 @@ __device__ void make_prim(const GeomParams& P, uint64_t slot, D3 s0, D3 s1, D3 s
 
 // line (context.go:283-294): a screen-space quad of width LineWidth as two
 // raster primitives, (v1,v0,v0; s11,s01,s00) and (v1,v1,v0; s10,s11,s00).
-__device__ void make_line_prims(const GeomParams& P, uint64_t slot, D3 s0, D3 s1, double r0, double r1,
-                                uint32_t v0, uint32_t v1, uint32_t elem) {
-    double lw2 = __ddiv_rn(P.st.line_width, 2.0);
+__device__ void make_line_prims(const GeomParams& P, double line_width, uint64_t slot, D3 s0, D3 s1, double r0,
+                                double r1, uint32_t v0, uint32_t v1, uint32_t elem) {
+    double lw2 = __ddiv_rn(line_width, 2.0);
     D3 d = sub3(s1, s0);
     D3 perp;  // Perpendicular (vector.go:179-187)
     if (d.x == 0 && d.y == 0) {
@@ -148,51 +155,32 @@ __device__ __forceinline__ int cull_decision(const StateView& st, double n0x, do
 
 // Emit the primitives of a triangle that survived culling: one, or six for
 // wireframe (context.go:296-301, 344-348).
-__device__ void emit_triangle(const GeomParams& P, uint64_t slot, D3 s0, D3 s1, D3 s2, double r0, double r1,
-                              double r2, uint32_t v0, uint32_t v1, uint32_t v2, uint32_t elem) {
-    if (P.st.wireframe) {
-        make_line_prims(P, slot + 0, s0, s1, r0, r1, v0, v1, elem);
-        make_line_prims(P, slot + 2, s1, s2, r1, r2, v1, v2, elem);
-        make_line_prims(P, slot + 4, s2, s0, r2, r0, v2, v0, elem);
+__device__ void emit_triangle(const GeomParams& P, const StateView& st, uint64_t slot, D3 s0, D3 s1, D3 s2,
+                              double r0, double r1, double r2, uint32_t v0, uint32_t v1, uint32_t v2, uint32_t elem) {
+    if (st.wireframe) {
+        make_line_prims(P, st.line_width, slot + 0, s0, s1, r0, r1, v0, v1, elem);
+        make_line_prims(P, st.line_width, slot + 2, s1, s2, r1, r2, v1, v2, elem);
+        make_line_prims(P, st.line_width, slot + 4, s2, s0, r2, r0, v2, v0, elem);
     } else {
         make_prim(P, slot, s0, s1, s2, r0, r1, r2, v0, v1, v2, elem);
     }
 }
 
 // ---------------------------------------------------------------------------
-// Triangle setup: one thread per triangle of [first, first+count).
+// Setup: one thread per element. The pass's setup tiles run draw by draw,
+// each draw's triangle tiles before its line tiles (DrawMesh draws lines after
+// triangles, context.go:435-439), and the ordered allocation runs across all
+// of them, so every draw's primitives are one contiguous, ordered range.
+// Triangles take one slot (six in wireframe), or 7x that when they need
+// clipping; lines always take two slots (dead when clipped away).
 // ---------------------------------------------------------------------------
-constexpr int kSetupBlock = 256;
-
-__global__ void __launch_bounds__(kSetupBlock) setup_triangles_kernel(GeomParams P) {
-    __shared__ uint32_t s_tile;
-    __shared__ OrderedAllocSmem<kSetupBlock> s_alloc;
-    const uint32_t tile = block_ticket<kSetupBlock>(P.lb_tri, &s_tile);
-    const uint64_t k = (uint64_t)tile * kSetupBlock + threadIdx.x;
-    const bool valid = k < P.tri_count;
-    const uint64_t t = P.tri_first + k;
-    const int per = P.st.wireframe ? 6 : 1;
-
-    uint32_t u0 = 0, u1 = 0, u2 = 0;
-    int order = 0;
-    bool clip = false;
-    if (valid) {
-        u0 = P.mesh.corner_uniq[3 * t + 0];
-        u1 = P.mesh.corner_uniq[3 * t + 1];
-        u2 = P.mesh.corner_uniq[3 * t + 2];
-        clip = (P.vout[u0] | P.vout[u1] | P.vout[u2]) != 0;
-        if (!clip) {
-            double2 n0 = P.vndc[u0], n1 = P.vndc[u1], n2 = P.vndc[u2];
-            order = cull_decision(P.st, n0.x, n0.y, n1.x, n1.y, n2.x, n2.y);
-        }
-    }
-    uint64_t count = !valid ? 0 : (clip ? (uint64_t)(7 * per) : (order != 0 ? (uint64_t)per : 0));
-    uint64_t slot = ordered_alloc<kSetupBlock>(P.lb_tri, tile, count, s_alloc);
-    if (!valid || count == 0) return;
+__device__ void setup_triangle(const GeomParams& P, const ItemView& I, uint32_t item, uint64_t k, uint64_t slot,
+                               uint64_t count, bool clip, int order, uint32_t u0, uint32_t u1, uint32_t u2) {
+    const uint64_t t = I.tri_first + k;
     if (clip) {
         uint32_t idx = atomicAdd(P.clip_count, 1u);
         if (idx < P.clip_cap) {
-            P.clip_list[idx] = make_ulonglong2(t, slot);
+            P.clip_list[idx] = ClipEntry{slot, (uint32_t)t, item};
         } else {
             atomicOr(P.status, ST_CLIP_OVERFLOW);
         }
@@ -203,37 +191,66 @@ __global__ void __launch_bounds__(kSetupBlock) setup_triangles_kernel(GeomParams
         uint32_t tu = u0; u0 = u2; u2 = tu;
         uint32_t tc = c0; c0 = c2; c2 = tc;
     }
-    VScreen a = P.vscr[u0], b = P.vscr[u1], c = P.vscr[u2];
-    emit_triangle(P, slot, d3(a.x, a.y, a.z), d3(b.x, b.y, b.z), d3(c.x, c.y, c.z), a.rw, b.rw, c.rw, c0, c1, c2,
-                  (uint32_t)t);
+    const VScreen* vscr = P.vscr + I.vbase;
+    VScreen a = vscr[u0], b = vscr[u1], c = vscr[u2];
+    emit_triangle(P, I.st, slot, d3(a.x, a.y, a.z), d3(b.x, b.y, b.z), d3(c.x, c.y, c.z), a.rw, b.rw, c.rw, c0, c1,
+                  c2, (uint32_t)t);
 }
 
-// ---------------------------------------------------------------------------
-// Line setup: one thread per line of [first, first+count). Lines always take
-// two slots (dead when clipped away); primitive slots continue after the
-// triangles' (DrawMesh draws lines after triangles, context.go:435-439).
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kSetupBlock) setup_lines_kernel(GeomParams P) {
+__global__ void __launch_bounds__(kSetupTile) setup_kernel(GeomParams P) {
     __shared__ uint32_t s_tile;
-    __shared__ OrderedAllocSmem<kSetupBlock> s_alloc;
-    const uint32_t tile = block_ticket<kSetupBlock>(P.lb_line, &s_tile);
-    const uint64_t k = (uint64_t)tile * kSetupBlock + threadIdx.x;
-    const bool valid = k < P.line_count;
-    const uint64_t l = P.line_first + k;
-    uint64_t count = valid ? 2 : 0;
-    uint64_t slot = ordered_alloc<kSetupBlock>(P.lb_line, tile, count, s_alloc);
-    if (!valid) return;
-    slot += *P.tri_slots;
-    const uint64_t cb = 3 * P.mesh.ntri + 2 * l;
-    uint32_t u0 = P.mesh.corner_uniq[cb], u1 = P.mesh.corner_uniq[cb + 1];
-    if ((P.vout[u0] | P.vout[u1]) != 0) {
-        uint32_t idx = atomicAdd(P.lclip_count, 1u);
-        P.lclip_list[idx] = make_ulonglong2(l, slot);  // lclip_list holds line_count entries
+    __shared__ OrderedAllocSmem<kSetupTile> s_alloc;
+    const uint32_t tile = block_ticket<kSetupTile>(P.lb, &s_tile);
+    const uint32_t item = find_item(P.starts.stile, P.nitems, tile);
+    const ItemView& I = P.items[item];
+    const uint32_t lt = tile - I.stile0;
+    const bool tri = lt < I.ntri_tiles;
+    const uint64_t k = (uint64_t)(tri ? lt : lt - I.ntri_tiles) * kSetupTile + threadIdx.x;
+    const bool valid = k < (tri ? I.tri_count : I.line_count);
+    const uint8_t* vout = P.vout + I.vbase;
+
+    uint64_t count = 0;
+    uint32_t u0 = 0, u1 = 0, u2 = 0;
+    int order = 0;
+    bool clip = false;
+    if (tri) {
+        const int per = I.st.wireframe ? 6 : 1;
+        if (valid) {
+            const uint64_t t = I.tri_first + k;
+            u0 = I.mesh.corner_uniq[3 * t + 0];
+            u1 = I.mesh.corner_uniq[3 * t + 1];
+            u2 = I.mesh.corner_uniq[3 * t + 2];
+            clip = (vout[u0] | vout[u1] | vout[u2]) != 0;
+            if (!clip) {
+                const double2* vndc = P.vndc + I.vbase;
+                double2 n0 = vndc[u0], n1 = vndc[u1], n2 = vndc[u2];
+                order = cull_decision(I.st, n0.x, n0.y, n1.x, n1.y, n2.x, n2.y);
+            }
+            count = clip ? (uint64_t)(7 * per) : (order != 0 ? (uint64_t)per : 0);
+        }
+    } else {
+        count = valid ? 2 : 0;
+    }
+    const uint64_t slot = ordered_alloc<kSetupTile>(P.lb, tile, count, s_alloc);
+    if (lt == 0 && threadIdx.x == 0) P.iout[item].prim_start = slot;  // thread 0's local prefix is 0
+    if (!valid || count == 0) return;
+    if (tri) {
+        setup_triangle(P, I, item, k, slot, count, clip, order, u0, u1, u2);
         return;
     }
-    VScreen a = P.vscr[u0], b = P.vscr[u1];
-    make_line_prims(P, slot, d3(a.x, a.y, a.z), d3(b.x, b.y, b.z), a.rw, b.rw, (uint32_t)cb, (uint32_t)(cb + 1),
-                    kLineFlag | (uint32_t)l);
+    const uint64_t l = I.line_first + k;
+    const uint64_t cb = 3 * I.mesh.ntri + 2 * l;
+    u0 = I.mesh.corner_uniq[cb];
+    u1 = I.mesh.corner_uniq[cb + 1];
+    if ((vout[u0] | vout[u1]) != 0) {
+        uint32_t idx = atomicAdd(P.lclip_count, 1u);
+        P.lclip_list[idx] = ClipEntry{slot, (uint32_t)l, item};  // lclip_list holds every line of the pass
+        return;
+    }
+    const VScreen* vscr = P.vscr + I.vbase;
+    VScreen a = vscr[u0], b = vscr[u1];
+    make_line_prims(P, I.st.line_width, slot, d3(a.x, a.y, a.z), d3(b.x, b.y, b.z), a.rw, b.rw, (uint32_t)cb,
+                    (uint32_t)(cb + 1), kLineFlag | (uint32_t)l);
 }
 
 // ---------------------------------------------------------------------------
@@ -334,21 +351,21 @@ __device__ void fix_normals(FullVertex& a, FullVertex& b, FullVertex& c) {
     if (c.nrm.x == 0 && c.nrm.y == 0 && c.nrm.z == 0) c.nrm = n;
 }
 
-__device__ FullVertex load_corner(const GeomParams& P, uint64_t corner) {
+__device__ FullVertex load_corner(const GeomParams& P, const ItemView& I, uint64_t corner) {
     FullVertex v;
-    APosNrm64 pn = P.mesh.pn64[corner];
+    const MeshView& M = I.mesh;
+    APosNrm64 pn = M.pn64[corner];
     v.pos = d3(pn.px, pn.py, pn.pz);
     v.nrm = d3(pn.nx, pn.ny, pn.nz);
-    v.tu = P.mesh.tex64 ? P.mesh.tex64[2 * corner] : 0.0;
-    v.tv = P.mesh.tex64 ? P.mesh.tex64[2 * corner + 1] : 0.0;
+    v.tu = M.tex64 ? M.tex64[2 * corner] : 0.0;
+    v.tv = M.tex64 ? M.tex64[2 * corner + 1] : 0.0;
     v.tz = 0.0;
-    if (P.mesh.col64) {
-        v.col = d4(P.mesh.col64[4 * corner], P.mesh.col64[4 * corner + 1], P.mesh.col64[4 * corner + 2],
-                   P.mesh.col64[4 * corner + 3]);
+    if (M.col64) {
+        v.col = d4(M.col64[4 * corner], M.col64[4 * corner + 1], M.col64[4 * corner + 2], M.col64[4 * corner + 3]);
     } else {
         v.col = d4(0, 0, 0, 0);
     }
-    VClip o = P.vclip[P.mesh.corner_uniq[corner]];
+    VClip o = P.vclip[I.vbase + M.corner_uniq[corner]];
     v.out = d4(o.x, o.y, o.z, o.w);
     return v;
 }
@@ -358,13 +375,14 @@ __device__ FullVertex load_corner(const GeomParams& P, uint64_t corner) {
 // [21e, 21e + 21).
 __global__ void __launch_bounds__(128) clip_triangles_kernel(GeomParams P) {
     uint32_t n = min(*P.clip_count, P.clip_cap);
-    const int per = P.st.wireframe ? 6 : 1;
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
-        ulonglong2 ent = P.clip_list[e];
-        uint64_t t = ent.x, base = ent.y;
-        const uint32_t mask = P.attr_mask;
+        const ClipEntry ent = P.clip_list[e];
+        const ItemView& I = P.items[ent.item];
+        const uint64_t t = ent.elem, base = ent.slot;
+        const int per = I.st.wireframe ? 6 : 1;
+        const uint32_t mask = I.attr_mask;
         FullVertex tv[3];
-        for (int c = 0; c < 3; c++) tv[c] = load_corner(P, 3 * t + c);
+        for (int c = 0; c < 3; c++) tv[c] = load_corner(P, I, 3 * t + c);
         if (mask & kAttrNrm) fix_normals(tv[0], tv[1], tv[2]);  // NewTriangle(v1, v2, v3)
         D3 p1 = d3(tv[0].out.x, tv[0].out.y, tv[0].out.z);
         D3 p2 = d3(tv[1].out.x, tv[1].out.y, tv[1].out.z);
@@ -401,7 +419,7 @@ __global__ void __launch_bounds__(128) clip_triangles_kernel(GeomParams P) {
             for (int c = 0; c < 3; c++) v[c].out = interp_out(tv[0], tv[1], tv[2], bw[c]);
             // drawClippedTriangle (context.go:316-349)
             D3 n0 = ndc_of(v[0].out), n1 = ndc_of(v[1].out), n2 = ndc_of(v[2].out);
-            int order = cull_decision(P.st, n0.x, n0.y, n1.x, n1.y, n2.x, n2.y);
+            int order = cull_decision(I.st, n0.x, n0.y, n1.x, n1.y, n2.x, n2.y);
             uint64_t slot = base + (uint64_t)sub * per;
             if (order == 0) {
                 for (int q = 0; q < per; q++) write_dead(P, slot + q);
@@ -420,10 +438,10 @@ __global__ void __launch_bounds__(128) clip_triangles_kernel(GeomParams P) {
             int i0 = 0, i2 = 2;
             if (order < 0) { i0 = 2; i2 = 0; }
             D3 nn[3] = {n0, n1, n2};
-            D3 s0 = screen_of_ndc(nn[i0], P.w2, P.h2);
-            D3 s1 = screen_of_ndc(nn[1], P.w2, P.h2);
-            D3 s2 = screen_of_ndc(nn[i2], P.w2, P.h2);
-            emit_triangle(P, slot, s0, s1, s2, __drcp_rn(v[i0].out.w), __drcp_rn(v[1].out.w),
+            D3 s0 = screen_of_ndc(nn[i0], I.w2, I.h2);
+            D3 s1 = screen_of_ndc(nn[1], I.w2, I.h2);
+            D3 s2 = screen_of_ndc(nn[i2], I.w2, I.h2);
+            emit_triangle(P, I.st, slot, s0, s1, s2, __drcp_rn(v[i0].out.w), __drcp_rn(v[1].out.w),
                           __drcp_rn(v[i2].out.w), pref[i0], pref[1], pref[i2], (uint32_t)t);
         }
         for (; sub < 7; sub++)
@@ -436,10 +454,12 @@ __global__ void __launch_bounds__(128) clip_triangles_kernel(GeomParams P) {
 __global__ void __launch_bounds__(128) clip_lines_kernel(GeomParams P) {
     uint32_t n = *P.lclip_count;
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
-        ulonglong2 ent = P.lclip_list[e];
-        uint64_t l = ent.x, slot = ent.y;
-        uint64_t cb = 3 * P.mesh.ntri + 2 * l;
-        VClip a = P.vclip[P.mesh.corner_uniq[cb]], b = P.vclip[P.mesh.corner_uniq[cb + 1]];
+        const ClipEntry ent = P.lclip_list[e];
+        const ItemView& I = P.items[ent.item];
+        const uint64_t l = ent.elem, slot = ent.slot;
+        uint64_t cb = 3 * I.mesh.ntri + 2 * l;
+        const VClip* vclip = P.vclip + I.vbase;
+        VClip a = vclip[I.mesh.corner_uniq[cb]], b = vclip[I.mesh.corner_uniq[cb + 1]];
         D4 w1 = d4(a.x, a.y, a.z, a.w), w2 = d4(b.x, b.y, b.z, b.w);
         bool culled = false;
         for (int k = 0; k < 6; k++) {
@@ -454,16 +474,18 @@ __global__ void __launch_bounds__(128) clip_lines_kernel(GeomParams P) {
             write_dead(P, slot + 1);
             continue;
         }
-        D3 s0 = screen_of_ndc(ndc_of(w1), P.w2, P.h2);
-        D3 s1 = screen_of_ndc(ndc_of(w2), P.w2, P.h2);
-        make_line_prims(P, slot, s0, s1, __ddiv_rn(1.0, w1.w), __ddiv_rn(1.0, w2.w), (uint32_t)cb,
+        D3 s0 = screen_of_ndc(ndc_of(w1), I.w2, I.h2);
+        D3 s1 = screen_of_ndc(ndc_of(w2), I.w2, I.h2);
+        make_line_prims(P, I.st.line_width, slot, s0, s1, __ddiv_rn(1.0, w1.w), __ddiv_rn(1.0, w2.w), (uint32_t)cb,
                         (uint32_t)(cb + 1), kLineFlag | (uint32_t)l);
     }
 }
 
-// Total primitive slots of the draw (triangles' then lines').
-__global__ void prim_total_kernel(GeomParams P) {
-    *P.prim_total = *P.tri_slots + *P.line_slots;
+// Each draw's primitive range ends where the next draw's begins (the last
+// ends at the pass total). One thread per draw.
+__global__ void prim_ranges_kernel(GeomParams P) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.nitems; i += gridDim.x * blockDim.x)
+        P.iout[i].prim_end = (i + 1 < P.nitems) ? P.iout[i + 1].prim_start : *P.prim_total;
 }
 
 }  // namespace fgc

@@ -7,24 +7,101 @@
 
 namespace fgc {
 
+// One draw of a pass: a mesh range, state, shader and target framebuffer,
+// with its place in the pass-wide arrays. A pass renders any number of
+// independent draws (views) with one launch per stage; a plain DrawMesh call
+// is a pass of one draw. The table lives in device memory; the lookup arrays
+// of ItemStarts map a global tile, block or band to its draw.
+struct __align__(16) ItemView {
+    MeshView mesh;
+    StateView st;
+    ShaderView sh;
+    uint64_t tri_first, tri_count, line_first, line_count;
+    double w2, h2;              // W/2, H/2 of the target (Screen matrix)
+    int32_t W, H;
+    int64_t N;                  // W*H
+    int32_t R;                  // rows per band
+    int32_t L;                  // pixels per band (R*W)
+    uint32_t nbands;            // bands of this draw
+    uint32_t band0;             // first pass-wide band
+    uint32_t nblk;              // binning blocks of this draw
+    uint32_t blk0;              // first pass-wide binning block
+    uint64_t mat0;              // first bin-matrix entry ([nbands][nblk])
+    uint64_t vbase;             // first vertex-stage record
+    uint32_t vtile0;            // first vertex tile
+    uint32_t stile0;            // first setup tile: triangle tiles, then line tiles
+    uint32_t ntri_tiles, nline_tiles;
+    uint32_t attr_mask;         // kAttr* bits the shader reads
+    int32_t clear_color_pending, clear_depth_pending;
+    uint32_t clear_color;
+    double clear_depth;
+    uint32_t* color;            // NRGBA, W*H
+    double* depth;              // W*H
+    uint32_t* winner;           // debug, or null
+    double* shaded;             // debug, or null
+};
+static_assert(sizeof(ItemView) % 16 == 0, "ItemView is copied in 16-byte words");
+
+// Per-draw results written by the device.
+struct ItemOut {
+    unsigned long long prim_start, prim_end;  // raster primitive slots [start, end)
+    unsigned long long info[4];               // total, updated, visited pixels, shaded fragments
+};
+
+// Starts of each draw's tiles / blocks / bands in the pass-wide numbering;
+// nitems + 1 entries each (the last is the total).
+struct ItemStarts {
+    const uint32_t* vtile;
+    const uint32_t* stile;
+    const uint32_t* blk;
+    const uint32_t* band;
+};
+
+// Index of the draw whose range [start[i], start[i+1]) holds key.
+__device__ __forceinline__ uint32_t find_item(const uint32_t* start, uint32_t nitems, uint32_t key) {
+    uint32_t lo = 0, hi = nitems - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= key) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// floor(x / W) for W > 0 in 32-bit arithmetic; most boxes lie inside the
+// frame, where it is 0 without a division.
+__device__ __forceinline__ int32_t floordiv_w(int32_t x, int32_t W) {
+    if ((uint32_t)x < (uint32_t)W) return 0;
+    int32_t q = x / W;
+    if (q * W != x && x < 0) q--;
+    return q;
+}
+
+// A clipped element: its primitive slots and draw.
+struct __align__(16) ClipEntry {
+    unsigned long long slot;    // first primitive slot
+    uint32_t elem;              // triangle (or line) index within the mesh
+    uint32_t item;
+};
+
 struct VertexParams {
-    const double* ux;
-    const double* uy;
-    const double* uz;
-    uint64_t n;
-    double m[16];
-    double w2, h2;
+    const ItemView* items;
+    ItemStarts starts;
+    uint32_t nitems;
+    uint32_t ntiles;            // vertex tiles of the pass (kVertexTile positions each)
     VClip* vclip;
     double2* vndc;
     VScreen* vscr;
     uint8_t* vout;
 };
+constexpr int kVertexTile = 256;
 
 struct GeomParams {
-    MeshView mesh;
-    StateView st;
-    double w2, h2;
-    uint64_t tri_first, tri_count, line_first, line_count;
+    const ItemView* items;
+    ItemStarts starts;
+    uint32_t nitems;
+    uint32_t ntiles;            // setup tiles of the pass
+    ItemOut* iout;
     const VClip* vclip;
     const double2* vndc;
     const VScreen* vscr;
@@ -33,30 +110,26 @@ struct GeomParams {
     PBox* pbox;
     uint32_t* pspan;            // per primitive: bound on covered pixels in one row
     uint64_t prim_cap;          // slots available in prims / pbox
-    ulonglong2* clip_list;      // (triangle, first slot)
+    ClipEntry* clip_list;       // clipped triangles
     uint32_t clip_cap;
     uint32_t* clip_count;
-    ulonglong2* lclip_list;     // (line, first slot), line_count entries
+    ClipEntry* lclip_list;      // clipped lines (capacity: all lines of the pass)
     uint32_t* lclip_count;
     PoolVertex* pool;           // 21 per clip_list entry
-    uint32_t attr_mask;         // kAttr* bits the shader reads
-    unsigned long long* tri_slots;
-    unsigned long long* line_slots;
     unsigned long long* prim_total;
-    Lookback lb_tri, lb_line;
+    Lookback lb;
     unsigned int* status;
 };
+constexpr int kSetupTile = 256;
 
 struct BinParams {
+    const ItemView* items;
+    ItemStarts starts;
+    uint32_t nitems;
+    const ItemOut* iout;
     const PBox* pbox;
-    const unsigned long long* nprim;
-    int32_t W;
-    int64_t N;
-    int64_t L;                  // pixels per band (R rows * W)
-    uint32_t nbands;
-    uint32_t nblk;              // blocks of the count/scatter grids
-    uint32_t* mat;              // [nbands][nblk] counts
-    uint32_t* off;              // [nbands][nblk] exclusive offsets
+    uint32_t* mat;              // per draw [nbands][nblk] counts, draws in order
+    uint32_t* off;              // exclusive offsets of mat
     const unsigned long long* pair_total;
     uint32_t* bins;
     uint64_t bin_cap;
@@ -71,41 +144,32 @@ struct ScanParams {
 };
 
 struct RasterParams {
+    const ItemView* items;
+    ItemStarts starts;
+    uint32_t nitems;
+    uint32_t nbands;            // bands of the pass
+    ItemOut* iout;
     const RPrim* prims;
     const PBox* pbox;
     const uint32_t* pspan;
     const uint32_t* bins;
-    const uint32_t* off;        // bin offsets: band b starts at off[b * nblk]
+    const uint32_t* off;        // bin offsets
+    uint64_t nmat;              // entries of off
     const unsigned long long* pair_total;
-    uint32_t nblk;
-    uint32_t nbands;
-    int32_t W, H;
-    int64_t N, L;
     int32_t F;                  // fragment buffer capacity
-    uint32_t* color;
-    double* depth;
-    int32_t clear_color_pending, clear_depth_pending;
-    uint32_t clear_color;
-    double clear_depth;
-    StateView st;
-    ShaderView sh;
-    MeshView mesh;
+    int32_t Lmax;               // largest band of the pass (depth staging)
     const PoolVertex* pool;
     unsigned int* band_counter;
     unsigned int* status;
-    unsigned long long* info;   // total, updated, visited pixels, shaded fragments
-    uint32_t* winner;           // debug, or null
-    double* shaded;             // debug, or null
-    double* dbg;                // debug scratch: gridDim * F * 4 doubles
+    double* dbg;                // debug scratch: gridDim * F * 4 doubles, or null
 };
 
 // Kernels (grid shapes chosen by the host runtime).
 __global__ void vertex_kernel(VertexParams P);
-__global__ void setup_triangles_kernel(GeomParams P);
-__global__ void setup_lines_kernel(GeomParams P);
+__global__ void setup_kernel(GeomParams P);
 __global__ void clip_triangles_kernel(GeomParams P);
 __global__ void clip_lines_kernel(GeomParams P);
-__global__ void prim_total_kernel(GeomParams P);
+__global__ void prim_ranges_kernel(GeomParams P);
 
 __global__ void bin_count_kernel(BinParams P);
 __global__ void scan_u32_kernel(ScanParams P);

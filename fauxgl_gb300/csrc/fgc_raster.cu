@@ -54,45 +54,50 @@ struct RasterSmem {
     unsigned long long* scratch;
 };
 
+// The band being rasterised: rows [r0, rend) of its draw's frame, pixels
+// [i0, i0 + npx) in linear index order.
 struct BandCtx {
-    int64_t i0, i1;
+    int64_t i0;
+    int32_t r0, rend;
+    int32_t npx;
     bool early;      // early depth rejection is valid
 };
 
 // ---------------------------------------------------------------------------
 // Attribute fetch
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void fetch_pn64(const RasterParams& P, uint32_t v, D3& pos, D3& nrm) {
+__device__ __forceinline__ void fetch_pn64(const RasterParams& P, const MeshView& M, uint32_t v, D3& pos, D3& nrm) {
     if (v & kPoolFlag) {
         const PoolVertex& q = P.pool[v & ~kPoolFlag];
         pos = d3(q.px, q.py, q.pz);
         nrm = d3(q.nx, q.ny, q.nz);
     } else {
-        APosNrm64 a = P.mesh.pn64[v];
+        APosNrm64 a = M.pn64[v];
         pos = d3(a.px, a.py, a.pz);
         nrm = d3(a.nx, a.ny, a.nz);
     }
 }
-__device__ __forceinline__ void fetch_tex64(const RasterParams& P, uint32_t v, double& u, double& w) {
+__device__ __forceinline__ void fetch_tex64(const RasterParams& P, const MeshView& M, uint32_t v, double& u,
+                                            double& w) {
     if (v & kPoolFlag) {
         const PoolVertex& q = P.pool[v & ~kPoolFlag];
         u = q.tu;
         w = q.tv;
-    } else if (P.mesh.tex64) {
-        u = P.mesh.tex64[2 * (uint64_t)v];
-        w = P.mesh.tex64[2 * (uint64_t)v + 1];
+    } else if (M.tex64) {
+        u = M.tex64[2 * (uint64_t)v];
+        w = M.tex64[2 * (uint64_t)v + 1];
     } else {
         u = 0.0;
         w = 0.0;
     }
 }
-__device__ __forceinline__ D4 fetch_col64(const RasterParams& P, uint32_t v) {
+__device__ __forceinline__ D4 fetch_col64(const RasterParams& P, const MeshView& M, uint32_t v) {
     if (v & kPoolFlag) {
         const PoolVertex& q = P.pool[v & ~kPoolFlag];
         return d4(q.cr, q.cg, q.cb, q.ca);
     }
-    if (P.mesh.col64) {
-        const double* c = P.mesh.col64 + 4 * (uint64_t)v;
+    if (M.col64) {
+        const double* c = M.col64 + 4 * (uint64_t)v;
         return d4(c[0], c[1], c[2], c[3]);
     }
     return d4(0, 0, 0, 0);
@@ -140,29 +145,30 @@ __device__ D4 bilinear64(const TexView& t, double u, double v) {  // texture.go:
     return c;
 }
 
-__device__ D4 shade64(const RasterParams& P, const RPrim& R, double b0, double b1, double b2) {
-    const ShaderView& S = P.sh;
+__device__ D4 shade64(const RasterParams& P, const ItemView& I, const RPrim& R, double b0, double b1, double b2) {
+    const ShaderView& S = I.sh;
+    const MeshView& M = I.mesh;
     if (S.kind == FGC_SHADER_SOLID_COLOR) return d4(S.color[0], S.color[1], S.color[2], S.color[3]);
     // perspective-correct barycentrics (context.go:236-237)
     D4 w = d4(__dmul_rn(b0, R.r0), __dmul_rn(b1, R.r1), __dmul_rn(b2, R.r2), 0.0);
     w.w = __drcp_rn(__dadd_rn(__dadd_rn(w.x, w.y), w.z));
     if (S.kind == FGC_SHADER_TEXTURE) {
         double u0, v0, u1, v1, u2, v2;
-        fetch_tex64(P, R.v0, u0, v0);
-        fetch_tex64(P, R.v1, u1, v1);
-        fetch_tex64(P, R.v2, u2, v2);
+        fetch_tex64(P, M, R.v0, u0, v0);
+        fetch_tex64(P, M, R.v1, u1, v1);
+        fetch_tex64(P, M, R.v2, u2, v2);
         return bilinear64(S.tex, interp1(u0, u1, u2, w), interp1(v0, v1, v2, w));
     }
     // PhongShader.Fragment (shader.go:75-96)
     D3 p0, n0, p1, n1, p2, n2;
-    fetch_pn64(P, R.v0, p0, n0);
-    fetch_pn64(P, R.v1, p1, n1);
-    fetch_pn64(P, R.v2, p2, n2);
+    fetch_pn64(P, M, R.v0, p0, n0);
+    fetch_pn64(P, M, R.v1, p1, n1);
+    fetch_pn64(P, M, R.v2, p2, n2);
     D3 pos = d3(interp1(p0.x, p1.x, p2.x, w), interp1(p0.y, p1.y, p2.y, w), interp1(p0.z, p1.z, p2.z, w));
     D3 nrm = normalize3(d3(interp1(n0.x, n1.x, n2.x, w), interp1(n0.y, n1.y, n2.y, w), interp1(n0.z, n1.z, n2.z, w)));
     D4 color;
     if (S.object_is_discard) {
-        D4 c0 = fetch_col64(P, R.v0), c1 = fetch_col64(P, R.v1), c2 = fetch_col64(P, R.v2);
+        D4 c0 = fetch_col64(P, M, R.v0), c1 = fetch_col64(P, M, R.v1), c2 = fetch_col64(P, M, R.v2);
         color = d4(interp1(c0.x, c1.x, c2.x, w), interp1(c0.y, c1.y, c2.y, w), interp1(c0.z, c1.z, c2.z, w),
                    interp1(c0.w, c1.w, c2.w, w));
     } else {
@@ -170,9 +176,9 @@ __device__ D4 shade64(const RasterParams& P, const RPrim& R, double b0, double b
     }
     if (S.has_texture) {
         double u0, v0, u1, v1, u2, v2;
-        fetch_tex64(P, R.v0, u0, v0);
-        fetch_tex64(P, R.v1, u1, v1);
-        fetch_tex64(P, R.v2, u2, v2);
+        fetch_tex64(P, M, R.v0, u0, v0);
+        fetch_tex64(P, M, R.v1, u1, v1);
+        fetch_tex64(P, M, R.v2, u2, v2);
         color = bilinear64(S.tex, interp1(u0, u1, u2, w), interp1(v0, v1, v2, w));
     }
     D3 L = d3(S.light[0], S.light[1], S.light[2]);
@@ -206,13 +212,13 @@ __device__ __forceinline__ float interpf(float a, float b, float c, float wx, fl
     return __fmaf_rn(c, wz, __fmaf_rn(b, wy, a * wx)) * ww;
 }
 
-__device__ __forceinline__ void fetch_pn32(const RasterParams& P, uint32_t v, F3& pos, F3& nrm) {
+__device__ __forceinline__ void fetch_pn32(const RasterParams& P, const MeshView& M, uint32_t v, F3& pos, F3& nrm) {
     if (v & kPoolFlag) {
         const PoolVertex& q = P.pool[v & ~kPoolFlag];
         pos = F3{(float)q.px, (float)q.py, (float)q.pz};
         nrm = F3{(float)q.nx, (float)q.ny, (float)q.nz};
     } else {
-        APosNrm32 a = P.mesh.pn32[v];
+        APosNrm32 a = M.pn32[v];
         pos = F3{a.px, a.py, a.pz};
         nrm = F3{a.nx, a.ny, a.nz};
     }
@@ -253,8 +259,9 @@ __device__ float powf_int_or_general(float x, float p) {
     return powf(x, p);
 }
 
-__device__ float4 shade32(const RasterParams& P, const RPrim& R, double b0, double b1, double b2) {
-    const ShaderView& S = P.sh;
+__device__ float4 shade32(const RasterParams& P, const ItemView& I, const RPrim& R, double b0, double b1, double b2) {
+    const ShaderView& S = I.sh;
+    const MeshView& M = I.mesh;
     if (S.kind == FGC_SHADER_SOLID_COLOR)
         return make_float4((float)S.color[0], (float)S.color[1], (float)S.color[2], (float)S.color[3]);
     float wx = (float)b0 * (float)R.r0, wy = (float)b1 * (float)R.r1, wz = (float)b2 * (float)R.r2;
@@ -269,9 +276,9 @@ __device__ float4 shade32(const RasterParams& P, const RPrim& R, double b0, doub
                 const PoolVertex& q = P.pool[vr[k] & ~kPoolFlag];
                 u[k] = (float)q.tu;
                 v[k] = (float)q.tv;
-            } else if (P.mesh.tex32) {
-                u[k] = P.mesh.tex32[2 * (uint64_t)vr[k]];
-                v[k] = P.mesh.tex32[2 * (uint64_t)vr[k] + 1];
+            } else if (M.tex32) {
+                u[k] = M.tex32[2 * (uint64_t)vr[k]];
+                v[k] = M.tex32[2 * (uint64_t)vr[k] + 1];
             } else {
                 u[k] = 0;
                 v[k] = 0;
@@ -282,9 +289,9 @@ __device__ float4 shade32(const RasterParams& P, const RPrim& R, double b0, doub
         have_color = true;
     }
     F3 p0, n0, p1, n1, p2, n2;
-    fetch_pn32(P, R.v0, p0, n0);
-    fetch_pn32(P, R.v1, p1, n1);
-    fetch_pn32(P, R.v2, p2, n2);
+    fetch_pn32(P, M, R.v0, p0, n0);
+    fetch_pn32(P, M, R.v1, p1, n1);
+    fetch_pn32(P, M, R.v2, p2, n2);
     F3 pos = F3{interpf(p0.x, p1.x, p2.x, wx, wy, wz, ww), interpf(p0.y, p1.y, p2.y, wx, wy, wz, ww),
                 interpf(p0.z, p1.z, p2.z, wx, wy, wz, ww)};
     F3 nrm = normf3(F3{interpf(n0.x, n1.x, n2.x, wx, wy, wz, ww), interpf(n0.y, n1.y, n2.y, wx, wy, wz, ww),
@@ -297,8 +304,8 @@ __device__ float4 shade32(const RasterParams& P, const RPrim& R, double b0, doub
                 if (vr[k] & kPoolFlag) {
                     const PoolVertex& q = P.pool[vr[k] & ~kPoolFlag];
                     c[k][0] = (float)q.cr; c[k][1] = (float)q.cg; c[k][2] = (float)q.cb; c[k][3] = (float)q.ca;
-                } else if (P.mesh.col32) {
-                    for (int j = 0; j < 4; j++) c[k][j] = P.mesh.col32[4 * (uint64_t)vr[k] + j];
+                } else if (M.col32) {
+                    for (int j = 0; j < 4; j++) c[k][j] = M.col32[4 * (uint64_t)vr[k] + j];
                 } else {
                     for (int j = 0; j < 4; j++) c[k][j] = 0;
                 }
@@ -342,16 +349,21 @@ __device__ __forceinline__ uint32_t u8_of_unit_f32(float c) {
 // ---------------------------------------------------------------------------
 // Row walk (context.go:184-278)
 // ---------------------------------------------------------------------------
+// A row walk in 32-bit band-relative coordinates: the pixel at x of the row
+// is band pixel rel + x, rel = (y - r0) * W. For a row that meets the band
+// (rows_in_band) and a box within the setup limits (|coordinates| <= 2^30,
+// extent <= 2^26), rel and rel + x stay far inside the int32 range.
 struct Walk {
-    int64_t x, x1, rowbase;
+    int32_t x, x1, rel;
     double w0, w1, w2;
     int32_t unit;
     bool was, done;
 };
 
-__device__ __forceinline__ void walk_init(Walk& s, const RPrim& R, const PBox& bx, int64_t y, int64_t W, int32_t unit) {
+__device__ __forceinline__ void walk_init(Walk& s, const RPrim& R, const PBox& bx, int32_t y, const BandCtx& B,
+                                          int32_t W, int32_t unit) {
     double w00 = R.w0, w01 = R.w1, w02 = R.w2;
-    for (int64_t j = bx.y0; j < y; j++) {  // w00 += b12 at the end of each earlier row
+    for (int32_t j = bx.y0; j < y; j++) {  // w00 += b12 at the end of each earlier row
         w00 = __dadd_rn(w00, R.b0);
         w01 = __dadd_rn(w01, R.b1);
         w02 = __dadd_rn(w02, R.b2);
@@ -363,27 +375,33 @@ __device__ __forceinline__ void walk_init(Walk& s, const RPrim& R, const PBox& b
     if (w00 < 0 && d0 > d) d = d0;
     if (w01 < 0 && d1 > d) d = d1;
     if (w02 < 0 && d2 > d) d = d2;
-    d = (double)go_f2i(d);
-    if (d < 0) d = 0;
+    int64_t di = go_f2i(d);  // d = float64(int(d)); if d < 0 { d = 0 }
+    if (di < 0) di = 0;
+    s.unit = unit;
+    s.was = false;
+    s.x1 = bx.x1;
+    s.rel = (y - B.r0) * W;
+    if (di > (int64_t)bx.x1 - bx.x0) {  // the row loop starts past x1
+        s.x = bx.x1 + 1;
+        s.done = true;
+        return;
+    }
+    d = (double)di;
     s.w0 = __dadd_rn(w00, __dmul_rn(R.a0, d));
     s.w1 = __dadd_rn(w01, __dmul_rn(R.a1, d));
     s.w2 = __dadd_rn(w02, __dmul_rn(R.a2, d));
-    s.x = (int64_t)bx.x0 + go_f2i(d);
-    s.x1 = bx.x1;
-    s.rowbase = y * W;
-    s.unit = unit;
-    s.was = false;
+    s.x = bx.x0 + (int32_t)di;
     s.done = false;
 }
 
 // Advance a walk, recording up to quota fragments. Returns the number of
 // covered in-band pixels (TotalPixels).
-__device__ __forceinline__ uint32_t walk_run(Walk& s, const RPrim& R, const RasterParams& P, const BandCtx& B,
-                                             RasterSmem& S, uint32_t* s_nfrag, uint32_t* s_conflict, int quota,
-                                             uint64_t& visited) {
+__device__ __forceinline__ uint32_t walk_run(Walk& s, const RPrim& R, const RasterParams& P, const ItemView& I,
+                                             const BandCtx& B, RasterSmem& S, uint32_t* s_nfrag,
+                                             uint32_t* s_conflict, int quota, uint64_t& visited) {
     uint32_t total = 0;
     int rec = 0;
-    const double bias = P.st.depth_bias;
+    const double bias = I.st.depth_bias;
     const double ra = R.ra;
     const RaSign rs = ra_sign(ra);
     while (s.x <= s.x1) {
@@ -393,7 +411,7 @@ __device__ __forceinline__ uint32_t walk_run(Walk& s, const RPrim& R, const Rast
         s.w0 = __dadd_rn(w0, R.a0);
         s.w1 = __dadd_rn(w1, R.a1);
         s.w2 = __dadd_rn(w2, R.a2);
-        const int64_t x = s.x++;
+        const int32_t x = s.x++;
         visited++;
         if (neg_product(w0, ra, rs) || neg_product(w1, ra, rs) || neg_product(w2, ra, rs)) {
             if (s.was) {
@@ -403,19 +421,19 @@ __device__ __forceinline__ uint32_t walk_run(Walk& s, const RPrim& R, const Rast
             continue;
         }
         s.was = true;
-        const int64_t i = s.rowbase + x;
-        if (i < 0) continue;
-        if (i >= B.i1) {  // beyond this band (and possibly the frame): no later pixel of the row is in it
+        // i = y*W + x is skipped outside [0, W*H) (context.go:223-228); here
+        // only this band's part of that range is drawn
+        const int32_t pix = s.rel + x;
+        if (pix >= B.npx) {  // beyond this band (and possibly the frame): no later pixel of the row is in it
             s.done = true;
             return total;
         }
-        if (i < B.i0) continue;
+        if (pix < 0) continue;
         total++;
         const double b0 = __dmul_rn(w0, ra);
         const double b1 = __dmul_rn(w1, ra);
         const double b2 = __dmul_rn(w2, ra);
         double z = __dadd_rn(__dadd_rn(__dmul_rn(b0, R.z0), __dmul_rn(b1, R.z1)), __dmul_rn(b2, R.z2));
-        const int pix = (int)(i - B.i0);
         if (B.early && __dadd_rn(z, bias) > S.depth[pix]) continue;
         uint32_t slot = atomicAdd(s_nfrag, 1u);
         if (slot >= (uint32_t)P.F) {  // the chunk's size bound did not hold: the chunk is redone
@@ -446,38 +464,38 @@ __device__ __forceinline__ uint32_t walk_run(Walk& s, const RPrim& R, const Rast
 // ---------------------------------------------------------------------------
 // Resolve
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void apply_fragment(const RasterParams& P, const BandCtx& B, RasterSmem& S, uint32_t f,
-                                               uint64_t& updated) {
+__device__ __forceinline__ void apply_fragment(const RasterParams& P, const ItemView& I, const BandCtx& B,
+                                               RasterSmem& S, uint32_t f, uint64_t& updated) {
     const uint8_t fl = S.fflag[f];
     if (fl & kFragDiscard) return;
     const uint32_t key = S.fkey[f];
     const int pix = (int)(key >> 16);
     const int unit = (int)(key & 0xffff);
     const double z = S.fz[f];
-    const double bz = __dadd_rn(z, P.st.depth_bias);
-    if (!P.st.read_depth || bz <= S.depth[pix]) {
+    const double bz = __dadd_rn(z, I.st.depth_bias);
+    if (!I.st.read_depth || bz <= S.depth[pix]) {
         updated++;
-        if (P.st.write_depth) S.depth[pix] = z;
-        if (P.st.write_color) {
+        if (I.st.write_depth) S.depth[pix] = z;
+        if (I.st.write_color) {
             // The colour buffer stays in global memory: the band is this
             // CTA's alone and one thread applies all of a pixel's fragments.
-            uint32_t* cp = P.color + B.i0 + pix;
+            uint32_t* cp = I.color + B.i0 + pix;
             if (fl & kFragBlend) {
                 *cp = blend_nrgba(*cp, S.fcol[f]);
             } else {
-                // SetNRGBA(x, y, c) ignores points outside the image rectangle
-                const int64_t i = B.i0 + pix;
-                const int64_t x = i - (int64_t)S.urow[unit] * P.W;
-                if (x >= 0 && x < P.W) *cp = S.fcol[f];
+                // SetNRGBA(x, y, c) ignores points outside the image rectangle:
+                // x = i - y*W with i = r0*W + pix
+                const int32_t x = pix - (S.urow[unit] - B.r0) * I.W;
+                if (x >= 0 && x < I.W) *cp = S.fcol[f];
             }
         }
-        if (P.winner) {
+        if (I.winner) {
             const uint32_t p = S.cprim[S.uslot[unit]];
-            P.winner[B.i0 + pix] = P.prims[p].elem;
+            I.winner[B.i0 + pix] = P.prims[p].elem;
         }
-        if (P.shaded) {
+        if (I.shaded) {
             const double* src = P.dbg + ((uint64_t)blockIdx.x * P.F + f) * 4;
-            double* dst = P.shaded + (uint64_t)(B.i0 + pix) * 4;
+            double* dst = I.shaded + (uint64_t)(B.i0 + pix) * 4;
             dst[0] = src[0];
             dst[1] = src[1];
             dst[2] = src[2];
@@ -487,7 +505,7 @@ __device__ __forceinline__ void apply_fragment(const RasterParams& P, const Band
 }
 
 template <int PREC>
-__device__ __forceinline__ void shade_fragment(const RasterParams& P, RasterSmem& S, uint32_t f) {
+__device__ __forceinline__ void shade_fragment(const RasterParams& P, const ItemView& I, RasterSmem& S, uint32_t f) {
     const uint32_t unit = S.fkey[f] & 0xffff;
     const RPrim& R = P.prims[S.cprim[S.uslot[unit]]];
     const double b0 = S.fb0[f], b1 = S.fb1[f], b2 = S.fb2[f];
@@ -495,16 +513,16 @@ __device__ __forceinline__ void shade_fragment(const RasterParams& P, RasterSmem
     uint32_t packed;
     double c[4];
     if (PREC == FGC_PRECISION_PLAIN) {
-        D4 col = shade64(P, R, b0, b1, b2);
+        D4 col = shade64(P, I, R, b0, b1, b2);
         c[0] = col.x; c[1] = col.y; c[2] = col.z; c[3] = col.w;
         if (dzero(col.x) && dzero(col.y) && dzero(col.z) && dzero(col.w)) fl |= kFragDiscard;
-        if (P.st.alpha_blend && dlt1(col.w)) fl |= kFragBlend;
+        if (I.st.alpha_blend && dlt1(col.w)) fl |= kFragBlend;
         packed = nrgba_pack_i(col.x, col.y, col.z, col.w);
     } else {
-        float4 col = shade32(P, R, b0, b1, b2);
+        float4 col = shade32(P, I, R, b0, b1, b2);
         c[0] = col.x; c[1] = col.y; c[2] = col.z; c[3] = col.w;
         if (col.x == 0 && col.y == 0 && col.z == 0 && col.w == 0) fl |= kFragDiscard;
-        if (P.st.alpha_blend && col.w < 1) fl |= kFragBlend;
+        if (I.st.alpha_blend && col.w < 1) fl |= kFragBlend;
         packed = u8_of_unit_f32(col.x) | (u8_of_unit_f32(col.y) << 8) | (u8_of_unit_f32(col.z) << 16) |
                  (u8_of_unit_f32(col.w) << 24);
     }
@@ -526,11 +544,11 @@ __device__ __forceinline__ void shade_fragment(const RasterParams& P, RasterSmem
 // by increasing key -- pixel, then unit -- selecting the next key from the
 // short list each time. The lists are emptied for the next chunk as they are
 // applied.
-__device__ void resolve_chunk(const RasterParams& P, const BandCtx& B, RasterSmem& S, uint32_t nfrag,
-                              bool conflict, uint64_t& updated) {
+__device__ void resolve_chunk(const RasterParams& P, const ItemView& I, const BandCtx& B, RasterSmem& S,
+                              uint32_t nfrag, bool conflict, uint64_t& updated) {
     if (!conflict) {
         for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) {
-            apply_fragment(P, B, S, f, updated);
+            apply_fragment(P, I, B, S, f, updated);
             S.head[bucket_of(S.fkey[f] >> 16)] = 0xFFFFu;
         }
         return;
@@ -557,7 +575,7 @@ __device__ void resolve_chunk(const RasterParams& P, const BandCtx& B, RasterSme
                 }
             }
             if (bestf == 0xFFFFu) break;
-            apply_fragment(P, B, S, bestf, updated);
+            apply_fragment(P, I, B, S, bestf, updated);
             last = best;
             first = false;
         }
@@ -568,31 +586,52 @@ __device__ void resolve_chunk(const RasterParams& P, const BandCtx& B, RasterSme
 // ---------------------------------------------------------------------------
 // Kernel
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void rows_in_band(const PBox& bx, int64_t W, int64_t i0, int64_t i1, int32_t& ylo,
+__device__ __forceinline__ void rows_in_band(const PBox& bx, int32_t W, const BandCtx& B, int32_t& ylo,
                                              int32_t& nrows) {
-    // rows y of the box whose index range [y*W + x0, y*W + x1] meets [i0, i1)
+    // Rows y of the box whose index range [y*W + x0, y*W + x1] meets the
+    // band's [r0*W, rend*W): y*W + x1 >= r0*W gives y >= r0 - floor(x1/W),
+    // y*W + x0 < rend*W gives y <= rend - 1 - floor(x0/W).
     if (bx.x0 > bx.x1) {
         ylo = 0;
         nrows = 0;
         return;
     }
-    int64_t a = floordiv(i0 - bx.x1 + W - 1, W);  // ceil((i0 - x1) / W)
-    int64_t b = floordiv(i1 - 1 - bx.x0, W);
+    int64_t a = (int64_t)B.r0 - floordiv_w(bx.x1, W);
+    int64_t b = (int64_t)B.rend - 1 - floordiv_w(bx.x0, W);
     if (a < bx.y0) a = bx.y0;
     if (b > bx.y1) b = bx.y1;
     ylo = (int32_t)a;
     nrows = (b >= a) ? (int32_t)(b - a + 1) : 0;
 }
 
+// Add the CTA's counters of one draw to the draw's totals and reset them
+// (all threads of the CTA call it together).
+__device__ __forceinline__ void flush_counters(const RasterParams& P, uint32_t item, uint64_t& tot, uint64_t& upd,
+                                               uint64_t& vis, uint64_t& shd) {
+    for (int o = 16; o > 0; o >>= 1) {
+        tot += __shfl_down_sync(0xffffffffu, tot, o);
+        upd += __shfl_down_sync(0xffffffffu, upd, o);
+        vis += __shfl_down_sync(0xffffffffu, vis, o);
+        shd += __shfl_down_sync(0xffffffffu, shd, o);
+    }
+    if ((threadIdx.x & 31) == 0 && item < P.nitems) {
+        unsigned long long* info = P.iout[item].info;
+        if (tot) atomicAdd(&info[0], (unsigned long long)tot);
+        if (upd) atomicAdd(&info[1], (unsigned long long)upd);
+        if (vis) atomicAdd(&info[2], (unsigned long long)vis);
+        if (shd) atomicAdd(&info[3], (unsigned long long)shd);
+    }
+    tot = upd = vis = shd = 0;
+}
+
 template <int PREC>
 __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int64_t L = P.L;
     const int F = P.F;
     RasterSmem S;
     {
         unsigned char* q = smem_raw;
-        S.depth = (double*)q; q += L * 8;
+        S.depth = (double*)q; q += (size_t)P.Lmax * 8;
         S.fb0 = (double*)q; q += (size_t)F * 8;
         S.fb1 = (double*)q; q += (size_t)F * 8;
         S.fb2 = (double*)q; q += (size_t)F * 8;
@@ -609,33 +648,52 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
         S.nxt = (unsigned short*)q; q += (size_t)F * 2;
         S.fflag = (uint8_t*)q;
     }
-    __shared__ uint32_t s_band, s_nfrag, s_conflict, s_nprim, s_nunit, s_big;
+    __shared__ uint32_t s_band, s_item, s_nfrag, s_conflict, s_nprim, s_nunit, s_big;
     __shared__ uint64_t s_warp[kRT / 32 + 1];
+    __shared__ ItemView s_iv;  // the draw of the current band
+    const ItemView& I = s_iv;
 
     if (*P.status & (ST_CLIP_OVERFLOW | ST_BIN_OVERFLOW | ST_LOOKBACK_TIMEOUT | ST_POOL_OVERFLOW)) return;
 
-    const bool early = P.st.read_depth && (!P.st.write_depth || P.st.depth_bias >= 0);
     const uint64_t pair_total = *P.pair_total;
     uint64_t tot = 0, upd = 0, vis = 0, shd = 0;
+    uint32_t cur = 0xFFFFFFFFu;  // the draw tot..shd count for
 
     for (;;) {
-        if (threadIdx.x == 0) s_band = atomicAdd(P.band_counter, 1u);
+        // the next band of the pass: bands run draw by draw, band by band
+        if (threadIdx.x == 0) {
+            const uint32_t g = atomicAdd(P.band_counter, 1u);
+            s_band = g;
+            s_item = (g < P.nbands) ? find_item(P.starts.band, P.nitems, g) : 0xFFFFFFFFu;
+        }
         __syncthreads();
-        const uint32_t band = s_band;
+        const uint32_t gband = s_band;
+        const uint32_t item = s_item;
+        if (gband >= P.nbands) break;
+        if (item != cur) {
+            flush_counters(P, cur, tot, upd, vis, shd);
+            cur = item;
+            const uint4* src = reinterpret_cast<const uint4*>(&P.items[item]);
+            uint4* dst = reinterpret_cast<uint4*>(&s_iv);
+            for (int j = threadIdx.x; j < (int)(sizeof(ItemView) / 16); j += blockDim.x) dst[j] = src[j];
+        }
         __syncthreads();
-        if (band >= P.nbands) break;
-        const uint64_t bstart = P.off[(uint64_t)band * P.nblk];
-        const uint64_t bend = (band + 1 < P.nbands) ? P.off[(uint64_t)(band + 1) * P.nblk] : pair_total;
+        const uint32_t band = gband - I.band0;
+        const uint64_t bstart = P.off[I.mat0 + (uint64_t)band * I.nblk];
+        const uint64_t mend = I.mat0 + (uint64_t)(band + 1) * I.nblk;  // the next band's (or draw's) first entry
+        const uint64_t bend = (mend < P.nmat) ? P.off[mend] : pair_total;
         const uint64_t bcount = bend - bstart;
-        if (bcount == 0 && !P.clear_color_pending && !P.clear_depth_pending) continue;
+        if (bcount == 0 && !I.clear_color_pending && !I.clear_depth_pending) continue;
         BandCtx B;
-        B.i0 = (int64_t)band * L;
-        B.i1 = min(B.i0 + L, P.N);
-        B.early = early;
-        const int npx = (int)(B.i1 - B.i0);
+        B.r0 = (int32_t)band * I.R;
+        B.rend = min(B.r0 + I.R, I.H);
+        B.i0 = (int64_t)B.r0 * I.W;
+        B.npx = (B.rend - B.r0) * I.W;
+        B.early = I.st.read_depth && (!I.st.write_depth || I.st.depth_bias >= 0);
+        const int npx = B.npx;
         for (int j = threadIdx.x; j < npx; j += blockDim.x) {
-            S.depth[j] = P.clear_depth_pending ? P.clear_depth : P.depth[B.i0 + j];
-            if (P.clear_color_pending) P.color[B.i0 + j] = P.clear_color;  // fused clear
+            S.depth[j] = I.clear_depth_pending ? I.clear_depth : I.depth[B.i0 + j];
+            if (I.clear_color_pending) I.color[B.i0 + j] = I.clear_color;  // fused clear
         }
         for (int j = threadIdx.x; j < kRasterHeads; j += blockDim.x) S.head[j] = 0xFFFFu;
         __syncthreads();
@@ -656,10 +714,10 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
             if (valid) {
                 p = P.bins[bstart + k + threadIdx.x];
                 bx = P.pbox[p];
-                rows_in_band(bx, P.W, B.i0, B.i1, ylo, nrows);
+                rows_in_band(bx, I.W, B, ylo, nrows);
                 int64_t wid = (int64_t)bx.x1 - bx.x0 + 1;
                 if (!box_bound && (int64_t)P.pspan[p] < wid) wid = P.pspan[p];
-                if (wid > L) wid = L;
+                if (wid > npx) wid = npx;
                 bound = (uint64_t)nrows * (uint64_t)wid;
             }
             uint64_t agg;
@@ -712,7 +770,7 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
             const int quota = big ? max(1, F / (int)max(nunit, 1u)) : 0x7fffffff;
             if (big && threadIdx.x < nunit) {
                 const uint32_t pp = S.cprim[0];
-                walk_init(wk, P.prims[pp], P.pbox[pp], S.urow[threadIdx.x], P.W, (int32_t)threadIdx.x);
+                walk_init(wk, P.prims[pp], P.pbox[pp], S.urow[threadIdx.x], B, I.W, (int32_t)threadIdx.x);
             }
             for (;;) {
                 if (threadIdx.x == 0) {
@@ -724,15 +782,15 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
                 if (big) {
                     if (threadIdx.x < nunit && !wk.done) {
                         const uint32_t pp = S.cprim[0];
-                        tchunk += walk_run(wk, P.prims[pp], P, B, S, &s_nfrag, &s_conflict, quota, vis);
+                        tchunk += walk_run(wk, P.prims[pp], P, I, B, S, &s_nfrag, &s_conflict, quota, vis);
                     }
                 } else {
                     for (uint32_t u = threadIdx.x; u < nunit; u += blockDim.x) {
                         const uint32_t pp = S.cprim[S.uslot[u]];
                         const RPrim& R = P.prims[pp];
                         Walk w2;
-                        walk_init(w2, R, P.pbox[pp], S.urow[u], P.W, (int32_t)u);
-                        tchunk += walk_run(w2, R, P, B, S, &s_nfrag, &s_conflict, 0x7fffffff, vis);
+                        walk_init(w2, R, P.pbox[pp], S.urow[u], B, I.W, (int32_t)u);
+                        tchunk += walk_run(w2, R, P, I, B, S, &s_nfrag, &s_conflict, 0x7fffffff, vis);
                     }
                 }
                 __syncthreads();
@@ -745,9 +803,9 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
                 tot += tchunk;
                 const uint32_t nfrag = s_nfrag;
                 if (threadIdx.x == 0) shd += nfrag;
-                for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) shade_fragment<PREC>(P, S, f);
+                for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) shade_fragment<PREC>(P, I, S, f);
                 __syncthreads();
-                resolve_chunk(P, B, S, nfrag, (s_conflict & 1u) != 0, upd);
+                resolve_chunk(P, I, B, S, nfrag, (s_conflict & 1u) != 0, upd);
                 __syncthreads();
                 const int more = big ? __syncthreads_or(threadIdx.x < nunit && !wk.done) : 0;
                 if (!more) break;
@@ -762,22 +820,10 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
             box_bound = false;
             k += nprim;
         }
-        for (int j = threadIdx.x; j < npx; j += blockDim.x) P.depth[B.i0 + j] = S.depth[j];
+        for (int j = threadIdx.x; j < npx; j += blockDim.x) I.depth[B.i0 + j] = S.depth[j];
         __syncthreads();
     }
-    // per-CTA counters
-    for (int o = 16; o > 0; o >>= 1) {
-        tot += __shfl_down_sync(0xffffffffu, tot, o);
-        upd += __shfl_down_sync(0xffffffffu, upd, o);
-        vis += __shfl_down_sync(0xffffffffu, vis, o);
-        shd += __shfl_down_sync(0xffffffffu, shd, o);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        if (tot) atomicAdd(&P.info[0], (unsigned long long)tot);
-        if (upd) atomicAdd(&P.info[1], (unsigned long long)upd);
-        if (vis) atomicAdd(&P.info[2], (unsigned long long)vis);
-        if (shd) atomicAdd(&P.info[3], (unsigned long long)shd);
-    }
+    flush_counters(P, cur, tot, upd, vis, shd);
 }
 
 const void* raster_kernel_ptr(int precision) {

@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define FGC_ABI_VERSION 1
+#define FGC_ABI_VERSION 2
 
 typedef enum fgc_status {
     FGC_OK = 0,
@@ -52,7 +52,8 @@ typedef enum fgc_status {
     FGC_ERR_CUDA = 3,               /* a CUDA runtime call failed                  */
     FGC_ERR_OUT_OF_MEMORY = 4,      /* device allocation failed                    */
     FGC_ERR_DEVICE_LIMIT = 5,       /* a kernel hit a bounded limit and gave up     */
-    FGC_ERR_UNSUPPORTED = 6         /* valid request outside what this build does  */
+    FGC_ERR_UNSUPPORTED = 6,        /* valid request outside what this build does  */
+    FGC_ERR_BUSY = 7                /* the context has draws in an unfinished batch */
 } fgc_status;
 
 /* Face and Cull take the reference's enum values (context.go:11-26). */
@@ -246,6 +247,62 @@ int fgc_context_set_stream(fgc_context* ctx, void* cuda_stream);
  * denominator of the FP64-bound stages (one add, multiply or compare is one
  * instruction). */
 int fgc_measure_fp64_rate(double* gops_per_s);
+
+/* ---- batches (no reference counterpart) --------------------------------- */
+/* A batch renders many independent draws -- views of uneven size, each with
+ * its own mesh range, state, shader and target context -- with one launch per
+ * pipeline stage for all of them: a persistent raster launch walks the
+ * (draw, band) queue of the whole batch. Every draw's output, RasterizeInfo
+ * included, is exactly what fgc_draw_triangles / fgc_draw_lines on its own
+ * would give. Draws run in list order; draws that share a context, or that
+ * differ in precision, go to successive passes of the same submission.
+ *
+ * fgc_batch_submit returns once the work is queued on the batch's stream;
+ * fgc_batch_wait blocks until it is done (re-running a pass whose buffers
+ * overflowed) and fills one fgc_rasterize_info per draw. Between the two, the
+ * contexts of the draws are busy: any other call on them returns
+ * FGC_ERR_BUSY. A draw with out_nrgba set has its frame copied there after
+ * the batch, box-downsampled by out_scale (1 = the frame itself; out_scale
+ * must divide the frame): (width/out_scale)*(height/out_scale)*4 bytes, best
+ * in page-locked memory. One submission is in flight per batch; use several
+ * batches (each with its own stream) to overlap submissions. */
+typedef struct fgc_batch fgc_batch;
+typedef struct fgc_batch_item {
+    fgc_context* context;
+    const fgc_mesh* mesh;
+    uint64_t tri_first, tri_count;    /* triangles [first, first+count)   */
+    uint64_t line_first, line_count;  /* then lines [first, first+count)  */
+    const fgc_state* state;
+    const fgc_shader* shader;
+    uint8_t* out_nrgba;               /* optional read-back destination    */
+    int32_t out_scale;                /* 0 or 1: no downsampling           */
+    int32_t reserved;
+} fgc_batch_item;
+/* Shapes of the batched pipeline. Results never depend on them;
+ * fgc_batch_autotune picks them by measurement. */
+typedef struct fgc_batch_tuning {
+    int32_t band_pixels;          /* raster band size in pixels, whole rows (default 4096) */
+    int32_t prims_per_bin_block;  /* primitives per binning block (default 4096)           */
+    int32_t fragment_cap;         /* fragment buffer of a raster CTA (default 1024)        */
+    int32_t use_graph;            /* 1: issue each submission as a CUDA graph              */
+} fgc_batch_tuning;
+int fgc_batch_create(fgc_batch** out);
+int fgc_batch_destroy(fgc_batch* b);
+int fgc_batch_set_stream(fgc_batch* b, void* cuda_stream);
+int fgc_batch_set_tuning(fgc_batch* b, const fgc_batch_tuning* t);
+int fgc_batch_get_tuning(const fgc_batch* b, fgc_batch_tuning* t);
+int fgc_batch_set_timing(fgc_batch* b, int32_t enable);
+int fgc_batch_submit(fgc_batch* b, const fgc_batch_item* items, uint64_t n);
+/* *done = 1 once the submitted work has finished on the device (no wait). */
+int fgc_batch_query(fgc_batch* b, int32_t* done);
+int fgc_batch_wait(fgc_batch* b, fgc_rasterize_info* infos);
+/* Counters (summed over the draws) and stage times of the last finished submission. */
+int fgc_batch_last_stats(const fgc_batch* b, fgc_stats* out);
+/* Render items `repeats` times under each candidate tuning, keep the fastest
+ * in the batch and write it to *best. The items' contexts are drawn into
+ * (clear them before real use). */
+int fgc_batch_autotune(fgc_batch* b, const fgc_batch_item* items, uint64_t n, int32_t repeats,
+                       fgc_batch_tuning* best);
 
 #ifdef __cplusplus
 }

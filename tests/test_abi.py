@@ -45,6 +45,8 @@ def test_struct_layouts_match_the_header(lib):
     assert ctypes.sizeof(_abi.FgcState) == 8 * 4 + 16
     assert ctypes.sizeof(_abi.FgcShader) == 8 + 8 * (16 + 4 + 3 + 3 + 4 + 4 + 4 + 1) + 8
     assert ctypes.sizeof(_abi.FgcRasterizeInfo) == 16
+    assert ctypes.sizeof(_abi.FgcBatchItem) == 8 * 2 + 8 * 4 + 8 * 3 + 4 * 2
+    assert ctypes.sizeof(_abi.FgcBatchTuning) == 16
 
 
 def test_defaults_without_gpu(lib):
@@ -57,7 +59,8 @@ def test_defaults_without_gpu(lib):
     lib.fgc_shader_phong(ctypes.byref(sh), m, (ctypes.c_double * 3)(0, 0, 1), (ctypes.c_double * 3)(0, 0, 5))
     assert sh.kind == _abi.FGC_SHADER_PHONG and sh.specular_power == 32.0
     assert list(sh.ambient_color) == [0.2, 0.2, 0.2, 1.0] and list(sh.diffuse_color) == [0.8, 0.8, 0.8, 1.0]
-    assert lib.fgc_abi_version() == 1
+    declared = int(re.search(r"#define FGC_ABI_VERSION (\d+)", open(HEADER).read()).group(1))
+    assert lib.fgc_abi_version() == declared
 
 
 def test_argument_errors_without_gpu(lib):
