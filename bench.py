@@ -67,9 +67,13 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ss-steps", type=int, default=5, help="timed frames of the 16x supersampled variants")
     ap.add_argument("--cpu-frames", type=int, default=5)
-    ap.add_argument("--only", choices=["all", "plain", "ss16"], default="all",
-                    help="plain / ss16: time only the plain 1080p frame or the plain 16x supersampled frame "
-                         "(for profiler runs)")
+    ap.add_argument("--batch-steps", type=int, default=5, help="timed batches of the 1,024-view thumbnail batch")
+    ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per rate of the serving loop")
+    ap.add_argument("--serve-max-requests", type=int, default=160, help="requests per rate at most")
+    ap.add_argument("--serve-budget-gb", type=int, default=96, help="HBM budget of the serving loop")
+    ap.add_argument("--only", choices=["all", "plain", "ss16", "batch", "serve"], default="all",
+                    help="plain / ss16 / batch: time only the plain 1080p frame, the plain 16x supersampled "
+                         "frame or the thumbnail batch (for profiler runs)")
     return ap.parse_args()
 
 
@@ -252,6 +256,236 @@ def time_frames(frame, steps, warmup, torch, dist_barrier, stage_acc=None):
     return e0.elapsed_time(e1) / steps, launches // max(steps, 1)
 
 
+BATCH_WORKLOAD = ("batched thumbnails: 256 seeded meshes (displaced icospheres, cylinders, cones; 200-200k "
+                  "triangles log-uniform, seed 3) x 4 cameras = 1,024 views at 256^2-1024^2, PhongShader with a "
+                  "random object colour, back-face culling, mixed precision, colour+depth clear per view")
+
+
+def bench_batch(lib, args, torch):
+    """Config-3 batch: every step renders all 1,024 views (clears included)
+    through fgc_batch_submit / fgc_batch_wait. Returns the 'batch' JSON object."""
+    import numpy as np
+    from fauxgl_gb300 import _abi, scenes
+    from fauxgl_gb300.context import _upload_mesh
+    from fauxgl_gb300.shader import NewPhongShader, to_fgc_shader
+    t0 = time.time()
+    meshes, views = scenes.thumbnail_batch()
+    handles = [_upload_mesh(m) for m in meshes]
+    log("batch scene: %d meshes, %d views, %d triangles drawn per batch (%.1fs)" % (
+        len(meshes), len(views), sum(meshes[v["mesh"]].ntri for v in views), time.time() - t0))
+    ctxs, keep = [], []
+    items = (_abi.FgcBatchItem * len(views))()
+    bg = (ctypes.c_double * 4)(*scenes.BACKGROUND)
+    out_bytes = 0
+    for i, v in enumerate(views):
+        c = ctypes.c_void_p()
+        _abi.check(lib.fgc_context_create(v["width"], v["height"], ctypes.byref(c)))
+        ctxs.append(c)
+        st = _abi.FgcState()
+        lib.fgc_state_default(ctypes.byref(st))
+        st.precision = _abi.FGC_PRECISION_MIXED
+        sh = NewPhongShader(v["matrix"], scenes.LIGHT, v["eye"])
+        sh.ObjectColor = v["color"]
+        shs = to_fgc_shader(sh)
+        keep += [st, shs]
+        m = meshes[v["mesh"]]
+        it = items[i]
+        it.context, it.mesh = c.value, handles[v["mesh"]]
+        it.tri_first, it.tri_count, it.line_first, it.line_count = 0, m.ntri, 0, m.nline
+        it.state, it.shader = ctypes.pointer(st), ctypes.pointer(shs)
+        out_bytes += v["width"] * v["height"] * 4
+    n = len(views)
+    b = ctypes.c_void_p()
+    _abi.check(lib.fgc_batch_create(ctypes.byref(b)))
+    stream = torch.cuda.current_stream()
+    _abi.check(lib.fgc_batch_set_stream(b, stream.cuda_stream))
+    infos = (_abi.FgcRasterizeInfo * n)()
+
+    def clears():
+        for c in ctxs:
+            lib.fgc_clear_color(c, bg)
+            lib.fgc_clear_depth(c, 1.7976931348623157e308)
+
+    def step():
+        clears()
+        _abi.check(lib.fgc_batch_submit(b, items, n))
+        _abi.check(lib.fgc_batch_wait(b, infos))
+
+    def timed(steps, warmup):
+        for _ in range(warmup):
+            step()
+        torch.cuda.synchronize()
+        lat = []
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            t = time.perf_counter()
+            step()
+            lat.append((time.perf_counter() - t) * 1e3)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps, lat
+
+    # autotune the pipeline shapes on this batch (results never depend on them)
+    tuned = _abi.FgcBatchTuning()
+    clears()
+    _abi.check(lib.fgc_batch_autotune(b, items, n, 1, ctypes.byref(tuned)))
+    tuning = {k: int(getattr(tuned, k)) for k, _ in _abi.FgcBatchTuning._fields_}
+    log("batch tuning:", tuning)
+    steps = max(3, args.batch_steps)
+    ms, lat = timed(steps, 2)
+    st = _abi.FgcStats()
+    _abi.check(lib.fgc_batch_last_stats(b, ctypes.byref(st)))
+    _abi.check(lib.fgc_batch_set_timing(b, 1))
+    step()
+    stt = _abi.FgcStats()
+    _abi.check(lib.fgc_batch_last_stats(b, ctypes.byref(stt)))
+    _abi.check(lib.fgc_batch_set_timing(b, 0))
+    # the same submission as a CUDA graph
+    tuned.use_graph = 1
+    _abi.check(lib.fgc_batch_set_tuning(b, ctypes.byref(tuned)))
+    g_ms, g_lat = timed(steps, 2)
+    tuned.use_graph = 0
+    _abi.check(lib.fgc_batch_set_tuning(b, ctypes.byref(tuned)))
+    # end to end: every view's frame read back into pinned host memory
+    pinned = torch.empty(out_bytes, dtype=torch.uint8, pin_memory=True)
+    base, off = pinned.data_ptr(), 0
+    for i, v in enumerate(views):
+        items[i].out_nrgba = base + off
+        items[i].out_scale = 1
+        off += v["width"] * v["height"] * 4
+    e_ms, e_lat = timed(steps, 1)
+    for i in range(n):
+        items[i].out_nrgba = None
+    # unbatched: the same views one fgc_draw_mesh each
+    info1 = _abi.FgcRasterizeInfo()
+    for c in ctxs:
+        _abi.check(lib.fgc_context_set_stream(c, stream.cuda_stream))
+
+    def one_by_one():
+        clears()
+        for i in range(n):
+            it = items[i]
+            _abi.check(lib.fgc_draw_triangles(ctxs[i], it.mesh, 0, it.tri_count, it.state, it.shader,
+                                              ctypes.byref(info1)))
+    one_by_one()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    one_by_one()
+    torch.cuda.synchronize()
+    single_ms = (time.perf_counter() - t) * 1e3
+    lib.fgc_batch_destroy(b)
+    for c in ctxs:
+        lib.fgc_context_destroy(c)
+    tris = sum(meshes[v["mesh"]].ntri for v in views)
+
+    def pct(x, q):
+        x = sorted(x)
+        return x[min(len(x) - 1, int(round(q * (len(x) - 1))))]
+    return {
+        "workload": BATCH_WORKLOAD, "views_per_batch": n, "triangles_per_batch": tris,
+        "value": round(n * 1e3 / ms, 1), "unit": "views/s", "ms_per_batch": round(ms, 3),
+        "latency_ms": {"p50": round(pct(lat, 0.5), 3), "p99": round(pct(lat, 0.99), 3), "steps": steps},
+        "mtri_per_s": round(tris / ms / 1e3, 1), "gfragments_per_s": round(st.covered_pixels / ms / 1e6, 3),
+        "graph": {"value": round(n * 1e3 / g_ms, 1), "ms_per_batch": round(g_ms, 3),
+                  "latency_ms": {"p50": round(pct(g_lat, 0.5), 3), "p99": round(pct(g_lat, 0.99), 3)}},
+        "e2e": {"value": round(n * 1e3 / e_ms, 1), "unit": "views/s", "ms_per_batch": round(e_ms, 3),
+                "latency_ms": {"p50": round(pct(e_lat, 0.5), 3), "p99": round(pct(e_lat, 0.99), 3)},
+                "d2h_bytes_per_step": out_bytes,
+                "h2d_bytes_per_step": n * (ctypes.sizeof(_abi.FgcState) + ctypes.sizeof(_abi.FgcShader))},
+        "unbatched": {"value": round(n * 1e3 / single_ms, 1), "ms_per_batch": round(single_ms, 3),
+                      "how": "the same views, one fgc_draw_triangles call each"},
+        "tuning": tuning, "dtype": "f64+f32",
+        "stages_ms": {k: round(v, 3) for k, v in zip(_abi.STAGE_NAMES, stt.stage_ms)},
+        "work": {"passes_kernel_launches": int(st.kernel_launches), "bands": int(st.bands),
+                 **{k: int(getattr(st, k)) for k in ("elements", "clipped", "primitives", "bin_entries",
+                                                     "visited_pixels", "covered_pixels", "shaded_fragments",
+                                                     "updated_pixels")}},
+    }
+
+
+SERVE_WORKLOAD = ("serving loop: pool of 64 resident meshes (displaced icospheres, 5k-1.31M triangles log-uniform, "
+                  "seed 4), Poisson arrivals, each request a random mesh, camera at radius 3, resolution in "
+                  "{512^2, 1920x1080, 3840x2160}, supersampling scale in {1, 2, 4} (box-downsampled on the "
+                  "device, result copied to the host), PhongShader with a random object colour")
+
+
+def _pool_mesh(args):
+    from fauxgl_gb300 import scenes
+    detail, seed = args
+    return scenes.displaced_sphere(detail, seed=seed)
+
+
+def serve_pool(n=64, seed=4, tri_min=5000, tri_max=1310720):
+    """The serving workload's resident meshes, built on all host cores."""
+    import math
+    import multiprocessing as mp
+    from fauxgl_gb300 import scenes
+    rng = scenes.SplitMix64(seed)
+    jobs = []
+    for i in range(n):
+        t = math.exp(math.log(tri_min) + rng.uniform() * (math.log(tri_max) - math.log(tri_min)))
+        detail = int(min(8, max(2, round(math.log(t / 20.0, 4)))))
+        jobs.append((detail, seed * 1000003 + i))
+    order = sorted(range(n), key=lambda i: -jobs[i][0])  # biggest first
+    with mp.get_context("spawn").Pool(min(n, os.cpu_count() or 1)) as p:
+        built = p.map(_pool_mesh, [jobs[i] for i in order], chunksize=1)
+    meshes = [None] * n
+    for i, m in zip(order, built):
+        meshes[i] = m
+    return meshes
+
+
+def serve_requests(meshes, n, seed):
+    import math
+    from fauxgl_gb300 import scenes
+    from fauxgl_gb300.geom import V, Vector
+    from fauxgl_gb300.serve import Request
+    rng = scenes.SplitMix64(seed)
+    sizes = [(512, 512), (1920, 1080), (3840, 2160)]
+    out = []
+    for _ in range(n):
+        mi = int(rng.uniform() * len(meshes))
+        az = 2 * math.pi * rng.uniform()
+        el = math.radians(-30.0 + 75.0 * rng.uniform())
+        eye = Vector(3 * math.cos(el) * math.cos(az), 3 * math.sin(el), 3 * math.cos(el) * math.sin(az))
+        w, h = sizes[int(rng.uniform() * 3)]
+        s = [1, 2, 4][int(rng.uniform() * 3)]
+        m = scenes.camera_matrix(w * s, h * s, eye=eye, center=V(0, 0, 0))
+        out.append(Request(mesh=mi, matrix=tuple(m), eye=tuple(eye),
+                           color=(rng.uniform(), rng.uniform(), rng.uniform(), 1.0), width=w, height=h, scale=s,
+                           light=tuple(scenes.LIGHT), background=tuple(scenes.BACKGROUND)))
+    return out
+
+
+def bench_serve(args, meshes):
+    """Config-4 serving loop at each arrival rate, mixed and plain forms."""
+    from fauxgl_gb300 import _abi
+    from fauxgl_gb300.serve import Server, latency_summary, poisson_arrivals, run_load
+    rates = [50, 200, 500, 1000, 2000]
+    out = {"workload": SERVE_WORKLOAD, "pool_triangles": sum(m.ntri for m in meshes), "rates": {}}
+    for form, prec in (("mixed", _abi.FGC_PRECISION_MIXED), ("plain", _abi.FGC_PRECISION_PLAIN)):
+        srv = Server(meshes, hbm_budget=args.serve_budget_gb << 30, slots=3, max_batch=32, precision=prec)
+        # warm-up: one request of each size class
+        warm = serve_requests(meshes, 6, seed=99)
+        run_load(srv, warm, [0.0] * len(warm))
+        res = {}
+        for k, rate in enumerate(rates):
+            arr = poisson_arrivals(float(rate), args.serve_seconds, seed=40 + k)[:args.serve_max_requests]
+            reqs = serve_requests(meshes, len(arr), seed=400 + k)
+            tickets, elapsed = run_load(srv, reqs, arr)
+            lat = latency_summary(tickets)
+            frags = sum(t.info[0] for t in tickets if t.done)
+            res[str(rate)] = {"requests": len(reqs), "elapsed_s": round(elapsed, 3),
+                              "frames_per_s": round(len(tickets) / elapsed, 2),
+                              "gfragments_per_s": round(frags / elapsed / 1e9, 3), **lat}
+            log("serve %s %4d req/s: %s" % (form, rate, res[str(rate)]))
+        out["rates"][form] = res
+        srv.trim()
+        del srv
+    return out
+
+
 def cpu_frames(mesh, nframes, nthreads):
     """The oracle's threaded form (the reference's own worker split) on the
     host cores: one warm-up frame, then the median of nframes."""
@@ -333,6 +567,9 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    # the serving pool is built by spawned workers before any GPU work
+    single = dist_env()[1] == 1  # the batch and serving workloads run at N=1 only
+    pool = serve_pool() if args.only in ("all", "serve") and args.serve_seconds > 0 and single else None
     import numpy as np
     import torch
     from fauxgl_gb300 import _abi
@@ -361,6 +598,12 @@ def main():
         ss_ms, _ = time_frames(f, args.steps, args.warmup, torch, barrier)
         print(json.dumps({"ss16_plain_ms_per_frame": round(ss_ms, 3), "steps": args.steps}), flush=True)
         f.close()
+        return 0
+    if args.only == "batch":
+        print(json.dumps({"batch": bench_batch(lib, args, torch)}), flush=True)
+        return 0
+    if args.only == "serve":
+        print(json.dumps({"serve": bench_serve(args, pool)}), flush=True)
         return 0
 
     # ---- headline: plain FP64 at 1080p, mesh resident ------------------------
@@ -419,6 +662,11 @@ def main():
                                       "overlay": {k: round(v / n, 3) for k, v in zip(_abi.STAGE_NAMES, f.pass_ms[1])}},
                         "work": {"surface": f.pass_work[0], "overlay": f.pass_work[1]}}
             f.close()
+    batch = serve = None
+    if args.only == "all" and args.batch_steps > 0 and single:
+        batch = bench_batch(lib, args, torch)
+    if args.only == "all" and pool is not None:
+        serve = bench_serve(args, pool)
     clocks.__exit__(None, None, None)
 
     # ---- roofline of the dominant stage --------------------------------------
@@ -484,6 +732,8 @@ def main():
             "mixed": ({"value": round(world * 1e3 / mixed_ms, 3), "unit": "frames/s", "dtype": "f64+f32"}
                       if mixed_ms else None),
             "ss16": ss,
+            "batch": batch,
+            "serve": serve,
             "clocks": clocks.summary(),
         }
         if cpu is not None:

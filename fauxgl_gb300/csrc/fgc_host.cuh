@@ -156,6 +156,7 @@ struct PassCounters {
     unsigned int pad0;
     unsigned long long prim_total;
     unsigned long long pair_total;
+    unsigned long long reserved;
 };
 
 // Tunable shapes of a pass; results do not depend on them.

@@ -199,19 +199,26 @@ __global__ void fp64_rate_kernel(double* out, double a, double b, int iters);
 // Pixel buckets of the raster kernel's per-chunk fragment lists.
 constexpr int kRasterHeads = 2048;
 
-// Dynamic shared memory of the raster kernel (layout in fgc_raster.cu):
-// depth[L] f64, b0/b1/b2/z[F] f64, scratch 64 u64,
-// key/colour/unit-slot/unit-row[F] u32, chunk tables 3*threads u32,
-// bucket list heads[kRasterHeads] u16, list links[F] u16, flags[F] u8.
-// The colour buffer is not staged: the band's pixels are read and written in
-// global memory by the CTA that owns them.
+// (primitive, row) units a chunk of wide primitives holds; a band has at most
+// this many rows.
+constexpr int kSpanUnits = 128;
+
+// Dynamic shared memory of the raster kernel (layout in fgc_raster.cu), for
+// a fragment buffer of F: depth[L] f64, fragment b0/b1/b2/z[F] f64, span
+// edge values[kSpanUnits] 3 x f64, scratch 64 u64, fragment key/colour[F]
+// u32, unit slot/row[F] u32, span x/count/offset[kSpanUnits] u32, chunk
+// primitives[threads] u32, bucket list heads[kRasterHeads] u16, list
+// links[F] u16, flags[F] u8. The colour buffer is not staged: the band's
+// pixels are read and written in global memory by the CTA that owns them.
 __host__ __device__ inline size_t raster_smem_bytes(int64_t L, int F, int threads) {
     size_t b = 0;
     b += (size_t)L * 8;
     b += (size_t)F * 8 * 4;
+    b += (size_t)kSpanUnits * 8 * 3;
     b += 64 * 8;
     b += (size_t)F * 4 * 4;
-    b += (size_t)threads * 4 * 3;
+    b += (size_t)kSpanUnits * 4 * 3;
+    b += (size_t)threads * 4;
     b += (size_t)kRasterHeads * 2;
     b += (size_t)F * 2;
     b += (size_t)F;

@@ -29,7 +29,6 @@ struct PassHeader {
     unsigned int status;  // submission-wide status word
     unsigned int pad[3];
     PassCounters c;
-    unsigned long long pad2;
 };
 static_assert(sizeof(PassHeader) == kHeaderBytes, "pass header layout");
 
@@ -62,7 +61,7 @@ struct PassPlan {
     uint64_t nmat = 0, nvert = 0, nlines = 0, prim_base = 0;
     int per_max = 1;
     bool any_tri = false, any_line = false, debug_shaded = false;
-    int32_t Lmax = 1, band_rows = 1;
+    int32_t Lmax = 1, band_rows = 1, Rmax = 1;
     int precision = FGC_PRECISION_PLAIN;
     int F = 0;
     size_t smem = 0;
@@ -142,7 +141,7 @@ int plan_pass(const Submission& sub, const std::vector<uint32_t>& idx, const Dev
         v.H = c->H;
         v.N = c->N;
         int64_t R = std::max<int64_t>(1, T.band_pixels / c->W);
-        R = std::min<int64_t>(R, kRasterThreads - 2);  // a band's rows of one primitive fit one CTA
+        R = std::min<int64_t>(R, kSpanUnits);  // a band's rows of one primitive fit one chunk
         R = std::min<int64_t>(R, c->H);
         if (R * c->W > 65535) return fail(FGC_ERR_UNSUPPORTED, "frame width above 65535 pixels is not supported");
         v.R = (int32_t)R;
@@ -181,6 +180,7 @@ int plan_pass(const Submission& sub, const std::vector<uint32_t>& idx, const Dev
         P.any_tri = P.any_tri || it.tc > 0;
         P.any_line = P.any_line || it.lc > 0;
         P.Lmax = std::max(P.Lmax, v.L);
+        P.Rmax = std::max(P.Rmax, v.R);
         if (j == 0) P.band_rows = v.R;
         v.attr_mask = 0;
         if (it.shv.kind == FGC_SHADER_PHONG) {

@@ -5,26 +5,30 @@
 // (vertex.go:18-47), the built-in Fragment shaders (shader.go:25-27, 44-46,
 // 75-96), BilinearSample (texture.go:41-63), Color.NRGBA (color.go:56-63).
 //
-// A persistent CTA takes bands from an atomic counter. A band's depth and
-// colour live in shared memory while its bin (raster primitives in
-// submission order) is processed in chunks:
-//   A1 walk   one thread per (primitive, row) unit replays rasterize's row
-//             loop exactly: the row's edge values are the serial sum of the
-//             per-row increments, the skip-ahead d, then the serial per-pixel
-//             adds with the inside test and the break after leaving the
-//             triangle. Every covered pixel of the band becomes a fragment
-//             (b0, b1, b2, z); an early depth test against the band's current
-//             depth drops fragments that cannot update (only when depth can
-//             only decrease during the draw).
-//   A2 shade  one thread per fragment: perspective-correct weights,
+// Persistent CTAs take (draw, band) work from an atomic counter. A band's
+// depth lives in shared memory and its colour in global memory (the band is
+// the CTA's alone) while its bin (raster primitives in submission order) is
+// processed in chunks of (primitive, row) units:
+//   fragments every covered pixel of the band becomes a fragment (b0, b1,
+//             b2, z) with exactly the edge values rasterize's serial row loop
+//             gives it. Narrow primitives: one thread per unit runs that loop
+//             (row start, skip-ahead d, per-pixel adds, inside test, break).
+//             Wide ones: one thread per unit finds the row's covered interval
+//             and its first edge values (exact jumps through the serial sums,
+//             fgc_fpjump.cuh), then all threads walk windows of kWin pixels.
+//             An early depth test against the band's current depth drops
+//             fragments that cannot update (only when depth can only
+//             decrease during the draw).
+//   shade     one thread per fragment: perspective-correct weights,
 //             interpolation and the built-in shader, in FP64 (plain) or FP32
 //             (mixed).
 //   resolve   fragments are applied per pixel in (primitive, row) order:
-//             directly when no two fragments of the chunk share a pixel,
-//             otherwise after a bitonic sort of (pixel, unit) keys, each
-//             pixel's run applied by one thread in order. The depth test,
+//             directly when no two fragments of the chunk share a pixel
+//             bucket, otherwise one thread per bucket list applies its
+//             fragments by increasing (pixel, unit) key. The depth test,
 //             UpdatedPixels, depth write and the NRGBA / alpha-blend colour
 //             write are exactly rasterize's (context.go:247-272).
+#include "fgc_fpjump.cuh"
 #include "fgc_internal.cuh"
 
 namespace fgc {
@@ -43,11 +47,15 @@ struct RasterSmem {
     double* fz;
     uint32_t* fkey;  // [F] (pixel << 16) | unit
     uint32_t* fcol;  // [F] NRGBA
-    uint32_t* uslot; // [F] unit -> chunk slot, flags in bits 24..
+    double* uw0;     // [kSpanUnits] unit -> edge values at its first covered in-band pixel
+    double* uw1;
+    double* uw2;
+    uint32_t* uslot; // [F] unit -> chunk slot
     int32_t* urow;   // [F] unit -> row y
+    int32_t* ux;     // [kSpanUnits] unit -> first covered in-band x
+    uint32_t* ucnt;  // [kSpanUnits] unit -> covered in-band pixels
+    uint32_t* ufrag; // [kSpanUnits] unit -> first fragment offset in the chunk
     uint32_t* cprim; // [kRT] chunk slot -> primitive
-    int32_t* cylo;   // [kRT]
-    int32_t* cnrow;  // [kRT]
     unsigned short* head;  // [kHeads] per pixel bucket: last fragment of its list (0xFFFF: none)
     unsigned short* nxt;   // [F] per fragment: the previous fragment in its bucket
     uint8_t* fflag;  // [F] discard / blend flags
@@ -347,26 +355,211 @@ __device__ __forceinline__ uint32_t u8_of_unit_f32(float c) {
 }
 
 // ---------------------------------------------------------------------------
-// Row walk (context.go:184-278)
+// Rows (context.go:184-278)
 // ---------------------------------------------------------------------------
-// A row walk in 32-bit band-relative coordinates: the pixel at x of the row
-// is band pixel rel + x, rel = (y - r0) * W. For a row that meets the band
+// rasterize walks each row serially: w_k += a_k per pixel, w0k += b_k per
+// row. Both sequences are monotone (round-to-nearest is monotone and a step
+// never moves against the sign of its addend), and so is w*ra for a fixed
+// ra; the coverage test "no b_k = w_k*ra is negative" is therefore true on
+// exactly one interval of the row, and the walk's break after leaving the
+// triangle never hides a later covered pixel. A row is handled as:
+//   span     one thread finds the row's covered interval exactly (a plain
+//            walk for short rows, the edges' sign changes located with exact
+//            jumps for long ones) and the edge values at its first pixel in
+//            the band;
+//   windows  the chunk's covered pixels, numbered in unit order, are dealt
+//            out kWin at a time; a window that starts inside a row starts
+//            from an exact jump (repeat_add) and walks on from there.
+// Every value is the one the serial walk would have had: the same adds in
+// the same order, only not all of them executed one after the other.
+constexpr int kWin = 8;          // fragment offsets one thread walks in a round
+constexpr int kNarrow = 32;      // boxes at most this wide are walked row by row
+constexpr int kShortRow = 40;    // rows of at most this many steps are walked plainly
+
+// Row state in 32-bit band-relative coordinates: the pixel at x of row y is
+// band pixel rel + x, rel = (y - r0) * W. For a row that meets the band
 // (rows_in_band) and a box within the setup limits (|coordinates| <= 2^30,
 // extent <= 2^26), rel and rel + x stay far inside the int32 range.
-struct Walk {
-    int32_t x, x1, rel;
-    double w0, w1, w2;
-    int32_t unit;
-    bool was, done;
+struct Span {
+    int32_t xa;        // first covered in-band x
+    int32_t cnt;       // covered in-band pixels
+    double w0, w1, w2; // edge values at xa
 };
 
-__device__ __forceinline__ void walk_init(Walk& s, const RPrim& R, const PBox& bx, int32_t y, const BandCtx& B,
-                                          int32_t W, int32_t unit) {
+// +1: w*ra can only rise along the row (an edge the row enters), -1: only
+// fall (an edge it leaves), 0: constant.
+__device__ __forceinline__ int edge_dir(double a, double ra) {
+    const unsigned long long ab = dbits(a), rb = dbits(ra);
+    if ((ab & kAbsMask) == 0 || bnan(ab) || (rb & kAbsMask) == 0 || bnan(rb)) return 0;
+    return ((ab ^ rb) >> 63) ? -1 : 1;
+}
+
+// First step t in (lo, hi] at which edge k's test "w*ra < 0" becomes `want`,
+// or hi + 1. The test is monotone in t and differs from `want` at lo. ws is
+// the edge value at step 0, q = 1/a.
+__device__ __noinline__ int64_t edge_flip(double ws, double a, double q, double ra, bool want, int64_t lo,
+                                          int64_t hi) {
+    const RaSign rs = ra_sign(ra);
+    if (lo >= hi) return hi + 1;
+    // the real-number crossing -ws/a is within a step or two of the exact one
+    // (q = 1/a may be infinite for a subnormal a: the estimate then falls
+    // outside (lo, hi] and the search starts at lo)
+    const int64_t e = go_f2i(__dmul_rn(-ws, q));
+    int64_t t = (e > lo + 2 && e - 2 <= hi) ? e - 2 : lo;
+    double w;
+    if (t > lo) {
+        w = repeat_add(ws, a, (uint64_t)t);
+        if (neg_product(w, ra, rs) == want) {
+            hi = t - 1;  // at or before t: search (lo, t]
+            int64_t L = lo, H = t;
+            while (H - L > 1) {
+                const int64_t mid = L + (H - L) / 2;
+                if (neg_product(repeat_add(ws, a, (uint64_t)mid), ra, rs) == want) H = mid;
+                else L = mid;
+            }
+            return H;
+        }
+        lo = t;
+    } else {
+        w = repeat_add(ws, a, (uint64_t)lo);
+    }
+    // a few plain steps from lo
+    for (int i = 0; i < 8; i++) {
+        if (lo >= hi) return hi + 1;
+        w = __dadd_rn(w, a);
+        lo++;
+        if (neg_product(w, ra, rs) == want) return lo;
+    }
+    // then halving over (lo, hi]
+    int64_t L = lo, H = hi + 1;
+    while (H - L > 1) {
+        const int64_t mid = L + (H - L) / 2;
+        if (neg_product(repeat_add(ws, a, (uint64_t)mid), ra, rs) == want) H = mid;
+        else L = mid;
+    }
+    return H;
+}
+
+// The covered in-band pixels of row y of a primitive: rasterize's row
+// prologue (row start, skip-ahead d) and its covered interval, clipped to
+// the band. visited counts the pixel steps taken one by one.
+__device__ __noinline__ Span row_span(const RPrim& R, const PBox& bx, int32_t y, int32_t r0, int32_t npx, int32_t W,
+                                      uint64_t& visited) {
+    Span sp;
+    sp.xa = 0;
+    sp.cnt = 0;
+    sp.w0 = sp.w1 = sp.w2 = 0;
+    // w00 after (y - y0) row increments
+    const uint64_t dy = (uint64_t)(y - bx.y0);
+    const double w00 = repeat_add(R.w0, R.b0, dy);
+    const double w01 = repeat_add(R.w1, R.b1, dy);
+    const double w02 = repeat_add(R.w2, R.b2, dy);
+    double d = 0;
+    double d0 = __dmul_rn(-w00, R.q0);
+    double d1 = __dmul_rn(-w01, R.q1);
+    double d2 = __dmul_rn(-w02, R.q2);
+    if (w00 < 0 && d0 > d) d = d0;
+    if (w01 < 0 && d1 > d) d = d1;
+    if (w02 < 0 && d2 > d) d = d2;
+    int64_t di = go_f2i(d);  // d = float64(int(d)); if d < 0 { d = 0 }
+    if (di < 0) di = 0;
+    const int64_t T = (int64_t)bx.x1 - bx.x0 - di;  // steps after the first: x = x0 + d .. x1
+    if (T < 0) return sp;
+    d = (double)di;
+    const double ws0 = __dadd_rn(w00, __dmul_rn(R.a0, d));
+    const double ws1 = __dadd_rn(w01, __dmul_rn(R.a1, d));
+    const double ws2 = __dadd_rn(w02, __dmul_rn(R.a2, d));
+    const int32_t xs = bx.x0 + (int32_t)di;
+    const double ra = R.ra;
+    const RaSign rs = ra_sign(ra);
+    int64_t ta, tb;  // covered steps [ta, tb]
+    double wa0, wa1, wa2;
+    if (T < kShortRow) {
+        // the plain walk, up to the break
+        double w0 = ws0, w1 = ws1, w2 = ws2;
+        ta = -1;
+        tb = T;
+        wa0 = wa1 = wa2 = 0;
+        for (int64_t t = 0; t <= T; t++) {
+            visited++;
+            const bool out = neg_product(w0, ra, rs) || neg_product(w1, ra, rs) || neg_product(w2, ra, rs);
+            if (out) {
+                if (ta >= 0) {
+                    tb = t - 1;
+                    break;
+                }
+            } else if (ta < 0) {
+                ta = t;
+                wa0 = w0;
+                wa1 = w1;
+                wa2 = w2;
+            }
+            w0 = __dadd_rn(w0, R.a0);
+            w1 = __dadd_rn(w1, R.a1);
+            w2 = __dadd_rn(w2, R.a2);
+        }
+        if (ta < 0) return sp;
+    } else {
+        // each edge's test changes at most once along the row
+        ta = 0;
+        tb = T;
+        const double ws[3] = {ws0, ws1, ws2};
+        const double as[3] = {R.a0, R.a1, R.a2};
+        const double qs[3] = {R.q0, R.q1, R.q2};
+#pragma unroll 1
+        for (int k = 0; k < 3; k++) {
+            const int dir = edge_dir(as[k], ra);
+            if (neg_product(ws[k], ra, rs)) {
+                if (dir <= 0) return sp;  // outside for the whole row
+                const int64_t e = edge_flip(ws[k], as[k], qs[k], ra, false, 0, T);
+                if (e > T) return sp;
+                if (e > ta) ta = e;
+            } else if (dir < 0) {
+                const int64_t e = edge_flip(ws[k], as[k], qs[k], ra, true, 0, T);
+                if (e - 1 < tb) tb = e - 1;
+            }
+        }
+        if (ta > tb) return sp;
+        wa0 = repeat_add(ws0, R.a0, (uint64_t)ta);
+        wa1 = repeat_add(ws1, R.a1, (uint64_t)ta);
+        wa2 = repeat_add(ws2, R.a2, (uint64_t)ta);
+        visited += 1;
+    }
+    // clip [xs + ta, xs + tb] to the band: pix = rel + x in [0, npx)
+    const int32_t rel = (y - r0) * W;
+    int64_t lo = (int64_t)xs + ta, hi = (int64_t)xs + tb;
+    if (lo < -(int64_t)rel) lo = -(int64_t)rel;
+    if (hi > (int64_t)npx - 1 - rel) hi = (int64_t)npx - 1 - rel;
+    if (lo > hi) return sp;
+    const uint64_t skip = (uint64_t)(lo - (xs + ta));
+    sp.xa = (int32_t)lo;
+    sp.cnt = (int32_t)(hi - lo + 1);
+    sp.w0 = repeat_add(wa0, R.a0, skip);
+    sp.w1 = repeat_add(wa1, R.a1, skip);
+    sp.w2 = repeat_add(wa2, R.a2, skip);
+    return sp;
+}
+
+// The fused walk for narrow primitives (rows of a few pixels, where finding
+// the span first would only repeat the adds): rasterize's row loop for row
+// y, recording every covered in-band pixel as a fragment. Returns the
+// covered in-band pixels (TotalPixels). A fragment beyond the buffer sets bit
+// 2 of *s_conflict: the chunk's size bound failed and the chunk is redone.
+__device__ __forceinline__ uint32_t walk_row(const RPrim& R, const PBox& bx, int32_t y, const RasterParams& P,
+                                             const ItemView& I, const BandCtx& B, RasterSmem& S, uint32_t unit,
+                                             uint32_t* s_nfrag, uint32_t* s_conflict, uint64_t& visited) {
+    const uint64_t dy = (uint64_t)(y - bx.y0);
     double w00 = R.w0, w01 = R.w1, w02 = R.w2;
-    for (int32_t j = bx.y0; j < y; j++) {  // w00 += b12 at the end of each earlier row
-        w00 = __dadd_rn(w00, R.b0);
-        w01 = __dadd_rn(w01, R.b1);
-        w02 = __dadd_rn(w02, R.b2);
+    if (dy <= 64) {
+        for (uint64_t j = 0; j < dy; j++) {  // w00 += b12 at the end of each earlier row
+            w00 = __dadd_rn(w00, R.b0);
+            w01 = __dadd_rn(w01, R.b1);
+            w02 = __dadd_rn(w02, R.b2);
+        }
+    } else {
+        w00 = repeat_add(w00, R.b0, dy);
+        w01 = repeat_add(w01, R.b1, dy);
+        w02 = repeat_add(w02, R.b2, dy);
     }
     double d = 0;
     double d0 = __dmul_rn(-w00, R.q0);
@@ -377,66 +570,41 @@ __device__ __forceinline__ void walk_init(Walk& s, const RPrim& R, const PBox& b
     if (w02 < 0 && d2 > d) d = d2;
     int64_t di = go_f2i(d);  // d = float64(int(d)); if d < 0 { d = 0 }
     if (di < 0) di = 0;
-    s.unit = unit;
-    s.was = false;
-    s.x1 = bx.x1;
-    s.rel = (y - B.r0) * W;
-    if (di > (int64_t)bx.x1 - bx.x0) {  // the row loop starts past x1
-        s.x = bx.x1 + 1;
-        s.done = true;
-        return;
-    }
+    if (di > (int64_t)bx.x1 - bx.x0) return 0;  // the row loop starts past x1
     d = (double)di;
-    s.w0 = __dadd_rn(w00, __dmul_rn(R.a0, d));
-    s.w1 = __dadd_rn(w01, __dmul_rn(R.a1, d));
-    s.w2 = __dadd_rn(w02, __dmul_rn(R.a2, d));
-    s.x = bx.x0 + (int32_t)di;
-    s.done = false;
-}
-
-// Advance a walk, recording up to quota fragments. Returns the number of
-// covered in-band pixels (TotalPixels).
-__device__ __forceinline__ uint32_t walk_run(Walk& s, const RPrim& R, const RasterParams& P, const ItemView& I,
-                                             const BandCtx& B, RasterSmem& S, uint32_t* s_nfrag,
-                                             uint32_t* s_conflict, int quota, uint64_t& visited) {
-    uint32_t total = 0;
-    int rec = 0;
+    double w0 = __dadd_rn(w00, __dmul_rn(R.a0, d));
+    double w1 = __dadd_rn(w01, __dmul_rn(R.a1, d));
+    double w2 = __dadd_rn(w02, __dmul_rn(R.a2, d));
+    const int32_t rel = (y - B.r0) * I.W;
     const double bias = I.st.depth_bias;
     const double ra = R.ra;
     const RaSign rs = ra_sign(ra);
-    while (s.x <= s.x1) {
-        // b_k = w_k * ra is negative exactly when neg_product says so; the
-        // products themselves are formed only for pixels that are used.
-        const double w0 = s.w0, w1 = s.w1, w2 = s.w2;
-        s.w0 = __dadd_rn(w0, R.a0);
-        s.w1 = __dadd_rn(w1, R.a1);
-        s.w2 = __dadd_rn(w2, R.a2);
-        const int32_t x = s.x++;
+    uint32_t total = 0;
+    bool was = false;
+    for (int32_t x = bx.x0 + (int32_t)di; x <= bx.x1; x++) {
+        const double c0 = w0, c1 = w1, c2 = w2;
+        w0 = __dadd_rn(c0, R.a0);
+        w1 = __dadd_rn(c1, R.a1);
+        w2 = __dadd_rn(c2, R.a2);
         visited++;
-        if (neg_product(w0, ra, rs) || neg_product(w1, ra, rs) || neg_product(w2, ra, rs)) {
-            if (s.was) {
-                s.done = true;
-                return total;
-            }
+        if (neg_product(c0, ra, rs) || neg_product(c1, ra, rs) || neg_product(c2, ra, rs)) {
+            if (was) break;
             continue;
         }
-        s.was = true;
+        was = true;
         // i = y*W + x is skipped outside [0, W*H) (context.go:223-228); here
         // only this band's part of that range is drawn
-        const int32_t pix = s.rel + x;
-        if (pix >= B.npx) {  // beyond this band (and possibly the frame): no later pixel of the row is in it
-            s.done = true;
-            return total;
-        }
+        const int32_t pix = rel + x;
+        if (pix >= B.npx) break;  // beyond this band: no later pixel of the row is in it
         if (pix < 0) continue;
         total++;
-        const double b0 = __dmul_rn(w0, ra);
-        const double b1 = __dmul_rn(w1, ra);
-        const double b2 = __dmul_rn(w2, ra);
-        double z = __dadd_rn(__dadd_rn(__dmul_rn(b0, R.z0), __dmul_rn(b1, R.z1)), __dmul_rn(b2, R.z2));
+        const double b0 = __dmul_rn(c0, ra);
+        const double b1 = __dmul_rn(c1, ra);
+        const double b2 = __dmul_rn(c2, ra);
+        const double z = __dadd_rn(__dadd_rn(__dmul_rn(b0, R.z0), __dmul_rn(b1, R.z1)), __dmul_rn(b2, R.z2));
         if (B.early && __dadd_rn(z, bias) > S.depth[pix]) continue;
-        uint32_t slot = atomicAdd(s_nfrag, 1u);
-        if (slot >= (uint32_t)P.F) {  // the chunk's size bound did not hold: the chunk is redone
+        const uint32_t slot = atomicAdd(s_nfrag, 1u);
+        if (slot >= (uint32_t)P.F) {
             atomicOr(s_conflict, 2u);
             continue;
         }
@@ -444,9 +612,7 @@ __device__ __forceinline__ uint32_t walk_run(Walk& s, const RPrim& R, const Rast
         S.fb1[slot] = b1;
         S.fb2[slot] = b2;
         S.fz[slot] = z;
-        S.fkey[slot] = ((uint32_t)pix << 16) | (uint32_t)s.unit;
-        // push onto the pixel's bucket list; a non-empty list means a
-        // possible conflict (same pixel or same bucket)
+        S.fkey[slot] = ((uint32_t)pix << 16) | unit;
         unsigned short* hd = &S.head[bucket_of((uint32_t)pix)];
         unsigned short old = *hd, assumed;
         do {
@@ -455,10 +621,45 @@ __device__ __forceinline__ uint32_t walk_run(Walk& s, const RPrim& R, const Rast
         } while (old != assumed);
         S.nxt[slot] = old;
         if (old != 0xFFFFu) atomicOr(s_conflict, 1u);
-        if (++rec == quota) return total;
     }
-    s.done = true;
     return total;
+}
+
+// Fragments of one piece of a row: len covered in-band pixels from band pixel pix,
+// edge values w at the first. Early depth rejection, fragment records, and
+// the push onto the pixel bucket lists (a non-empty list is a possible
+// conflict: same pixel or same bucket).
+__device__ __forceinline__ void emit_segment(const RPrim& R, const ItemView& I, const BandCtx& B, RasterSmem& S,
+                                             int32_t pix, int32_t len, double w0, double w1, double w2, uint32_t unit,
+                                             uint32_t* s_nfrag, uint32_t* s_conflict) {
+    const double bias = I.st.depth_bias;
+    const double ra = R.ra;
+    for (int32_t i = 0; i < len; i++, pix++) {
+        const double b0 = __dmul_rn(w0, ra);
+        const double b1 = __dmul_rn(w1, ra);
+        const double b2 = __dmul_rn(w2, ra);
+        if (i + 1 < len) {
+            w0 = __dadd_rn(w0, R.a0);
+            w1 = __dadd_rn(w1, R.a1);
+            w2 = __dadd_rn(w2, R.a2);
+        }
+        const double z = __dadd_rn(__dadd_rn(__dmul_rn(b0, R.z0), __dmul_rn(b1, R.z1)), __dmul_rn(b2, R.z2));
+        if (B.early && __dadd_rn(z, bias) > S.depth[pix]) continue;
+        const uint32_t slot = atomicAdd(s_nfrag, 1u);  // below F: the round was sized for every pixel
+        S.fb0[slot] = b0;
+        S.fb1[slot] = b1;
+        S.fb2[slot] = b2;
+        S.fz[slot] = z;
+        S.fkey[slot] = ((uint32_t)pix << 16) | unit;
+        unsigned short* hd = &S.head[bucket_of((uint32_t)pix)];
+        unsigned short old = *hd, assumed;
+        do {
+            assumed = old;
+            old = atomicCAS(hd, assumed, (unsigned short)slot);
+        } while (old != assumed);
+        S.nxt[slot] = old;
+        if (old != 0xFFFFu) atomicOr(s_conflict, 1u);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -636,19 +837,23 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
         S.fb1 = (double*)q; q += (size_t)F * 8;
         S.fb2 = (double*)q; q += (size_t)F * 8;
         S.fz = (double*)q; q += (size_t)F * 8;
+        S.uw0 = (double*)q; q += (size_t)kSpanUnits * 8;
+        S.uw1 = (double*)q; q += (size_t)kSpanUnits * 8;
+        S.uw2 = (double*)q; q += (size_t)kSpanUnits * 8;
         S.scratch = (unsigned long long*)q; q += 64 * 8;
         S.fkey = (uint32_t*)q; q += (size_t)F * 4;
         S.fcol = (uint32_t*)q; q += (size_t)F * 4;
         S.uslot = (uint32_t*)q; q += (size_t)F * 4;
         S.urow = (int32_t*)q; q += (size_t)F * 4;
+        S.ux = (int32_t*)q; q += (size_t)kSpanUnits * 4;
+        S.ucnt = (uint32_t*)q; q += (size_t)kSpanUnits * 4;
+        S.ufrag = (uint32_t*)q; q += (size_t)kSpanUnits * 4;
         S.cprim = (uint32_t*)q; q += kRT * 4;
-        S.cylo = (int32_t*)q; q += kRT * 4;
-        S.cnrow = (int32_t*)q; q += kRT * 4;
         S.head = (unsigned short*)q; q += (size_t)kRasterHeads * 2;
         S.nxt = (unsigned short*)q; q += (size_t)F * 2;
         S.fflag = (uint8_t*)q;
     }
-    __shared__ uint32_t s_band, s_item, s_nfrag, s_conflict, s_nprim, s_nunit, s_big;
+    __shared__ uint32_t s_band, s_item, s_nfrag, s_conflict, s_nprim, s_nunit, s_ftotal, s_mode;
     __shared__ uint64_t s_warp[kRT / 32 + 1];
     __shared__ ItemView s_iv;  // the draw of the current band
     const ItemView& I = s_iv;
@@ -699,125 +904,176 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
         __syncthreads();
 
         uint64_t k = 0;
-        bool box_bound = false;  // size the next chunk by bounding boxes only
+        bool box_bound = false;  // size the next direct chunk by bounding boxes only
         while (k < bcount) {
-            // ---- chunk formation: a prefix of the remaining bin whose
-            // fragment bound fits the buffer. A row of a primitive holds at
-            // most pspan covered pixels (its widest chord, set up in
-            // make_prim); box_bound falls back to the bounding-box width
-            // after a chunk whose walk outgrew the buffer.
+            // ---- chunk: a prefix of the remaining bin, at most one primitive
+            // per thread. Its first primitive picks how it is walked:
+            //   direct  narrow primitives, each row walked and recorded by one
+            //           thread as rasterize does; the prefix also keeps a bound
+            //           on its fragments within F (a row holds at most pspan,
+            //           its widest chord, covered pixels; box_bound falls back
+            //           to the box width after a chunk whose walk outgrew F)
+            //   spans   anything else, at most kSpanUnits units: spans, then
+            //           windows of fragment offsets
             uint32_t p = 0;
-            PBox bx{1, 0, 1, 0};
             int32_t ylo = 0, nrows = 0;
             uint64_t bound = 0;
+            bool narrow = true;
             const bool valid = (k + threadIdx.x) < bcount;
             if (valid) {
                 p = P.bins[bstart + k + threadIdx.x];
-                bx = P.pbox[p];
+                const PBox bx = P.pbox[p];
                 rows_in_band(bx, I.W, B, ylo, nrows);
                 int64_t wid = (int64_t)bx.x1 - bx.x0 + 1;
+                narrow = wid <= kNarrow;
                 if (!box_bound && (int64_t)P.pspan[p] < wid) wid = P.pspan[p];
                 if (wid > npx) wid = npx;
+                if (wid < 0) wid = 0;
                 bound = (uint64_t)nrows * (uint64_t)wid;
             }
-            uint64_t agg;
-            uint64_t excl = block_exclusive_scan<kRT>(bound, s_warp, &agg);
-            const bool take = valid && (excl + bound <= (uint64_t)F);
-            // units of the taken primitives (the taken set is a prefix)
-            uint64_t uagg;
-            uint64_t ubase = block_exclusive_scan<kRT>(take ? (uint64_t)nrows : 0, s_warp, &uagg);
+            if (threadIdx.x == 0) s_mode = (narrow && bound <= (uint64_t)F) ? 1u : 0u;
+            __syncthreads();
+            const bool direct = s_mode != 0;
+            const uint64_t key = !direct ? 0 : (valid && narrow) ? bound : (uint64_t)F + 1;
+            uint64_t bagg, uagg;
+            const uint64_t bexcl = block_exclusive_scan<kRT>(key, s_warp, &bagg);
+            const uint64_t ubase = block_exclusive_scan<kRT>(valid ? (uint64_t)nrows : 0, s_warp, &uagg);
+            // a prefix, never empty (R <= kSpanUnits; a direct chunk's first
+            // bound <= F, and its units are at most its bound)
+            const uint64_t ucap = direct ? (uint64_t)F : (uint64_t)kSpanUnits;
+            const bool take = valid && ubase + (uint64_t)nrows <= ucap && bexcl + key <= (uint64_t)F;
             if (threadIdx.x == 0) {
                 s_nprim = 0;
-                s_big = 0;
+                s_nunit = 0;
             }
             __syncthreads();
             if (take) {
                 atomicAdd(&s_nprim, 1u);
+                atomicAdd(&s_nunit, (uint32_t)nrows);
                 S.cprim[threadIdx.x] = p;
-                S.cylo[threadIdx.x] = ylo;
-                S.cnrow[threadIdx.x] = nrows;
                 for (int r = 0; r < nrows; r++) {
                     S.uslot[ubase + r] = threadIdx.x;
                     S.urow[ubase + r] = ylo + r;
                 }
             }
             __syncthreads();
-            uint32_t nprim = s_nprim;
-            uint32_t nunit = (uint32_t)uagg;
-            bool big = false;
-            if (nprim == 0) {
-                // the next primitive alone exceeds the buffer: walk its rows in
-                // rounds of at most F fragments
-                big = true;
-                nprim = 1;
-                if (threadIdx.x == 0) {
-                    S.cprim[0] = p;
-                    S.cylo[0] = ylo;
-                    S.cnrow[0] = nrows;
-                }
-                __syncthreads();
-                nunit = (uint32_t)S.cnrow[0];
-                for (uint32_t r = threadIdx.x; r < nunit; r += blockDim.x) {
-                    S.uslot[r] = 0;
-                    S.urow[r] = S.cylo[0] + (int32_t)r;
-                }
-            }
-            __syncthreads();
+            const uint32_t nprim = s_nprim, nunit = s_nunit;
 
-            // ---- A1 / A2 / resolve, in rounds (one round unless big)
-            Walk wk;
-            wk.done = true;
-            const int quota = big ? max(1, F / (int)max(nunit, 1u)) : 0x7fffffff;
-            if (big && threadIdx.x < nunit) {
-                const uint32_t pp = S.cprim[0];
-                walk_init(wk, P.prims[pp], P.pbox[pp], S.urow[threadIdx.x], B, I.W, (int32_t)threadIdx.x);
-            }
-            for (;;) {
+            if (direct) {
                 if (threadIdx.x == 0) {
                     s_nfrag = 0;
                     s_conflict = 0;
                 }
                 __syncthreads();
                 uint64_t tchunk = 0;
-                if (big) {
-                    if (threadIdx.x < nunit && !wk.done) {
-                        const uint32_t pp = S.cprim[0];
-                        tchunk += walk_run(wk, P.prims[pp], P, I, B, S, &s_nfrag, &s_conflict, quota, vis);
-                    }
-                } else {
-                    for (uint32_t u = threadIdx.x; u < nunit; u += blockDim.x) {
-                        const uint32_t pp = S.cprim[S.uslot[u]];
-                        const RPrim& R = P.prims[pp];
-                        Walk w2;
-                        walk_init(w2, R, P.pbox[pp], S.urow[u], B, I.W, (int32_t)u);
-                        tchunk += walk_run(w2, R, P, I, B, S, &s_nfrag, &s_conflict, 0x7fffffff, vis);
-                    }
+                for (uint32_t u = threadIdx.x; u < nunit; u += blockDim.x) {
+                    const uint32_t pp = S.cprim[S.uslot[u]];
+                    tchunk += walk_row(P.prims[pp], P.pbox[pp], S.urow[u], P, I, B, S, u, &s_nfrag, &s_conflict, vis);
                 }
                 __syncthreads();
-                if (s_conflict & 2u) {  // overflow: nothing was applied; empty the lists, redo with box bounds
+                const bool redo = (s_conflict & 2u) != 0;
+                if (redo) {  // nothing was applied: empty the lists, redo with box bounds
                     const uint32_t nrec = min(s_nfrag, (uint32_t)F);
                     for (uint32_t f = threadIdx.x; f < nrec; f += blockDim.x)
                         S.head[bucket_of(S.fkey[f] >> 16)] = 0xFFFFu;
-                    break;
+                } else {
+                    tot += tchunk;
+                    const uint32_t nfrag = s_nfrag;
+                    if (threadIdx.x == 0) shd += nfrag;
+                    for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) shade_fragment<PREC>(P, I, S, f);
+                    __syncthreads();
+                    resolve_chunk(P, I, B, S, nfrag, (s_conflict & 1u) != 0, upd);
                 }
-                tot += tchunk;
+                __syncthreads();
+                if (redo && !box_bound) {
+                    box_bound = true;
+                    continue;
+                }
+                if (redo && threadIdx.x == 0) atomicOr(P.status, ST_RASTER_INTERNAL);
+                box_bound = false;
+                k += nprim;
+                continue;
+            }
+            box_bound = false;
+
+            // ---- spans: each unit's covered in-band pixels
+            for (uint32_t u = threadIdx.x; u < nunit; u += blockDim.x) {
+                const uint32_t pp = S.cprim[S.uslot[u]];
+                const Span sp = row_span(P.prims[pp], P.pbox[pp], S.urow[u], B.r0, B.npx, I.W, vis);
+                S.ux[u] = sp.xa;
+                S.ucnt[u] = (uint32_t)sp.cnt;
+                S.uw0[u] = sp.w0;
+                S.uw1[u] = sp.w1;
+                S.uw2[u] = sp.w2;
+                tot += (uint64_t)sp.cnt;
+            }
+            __syncthreads();
+            // ---- fragment offsets of the units, in unit order
+            {
+                const uint32_t per = ((uint32_t)kSpanUnits + kRT - 1) / kRT;
+                const uint32_t u0 = threadIdx.x * per;
+                uint64_t local = 0;
+                for (uint32_t j = 0; j < per; j++)
+                    if (u0 + j < nunit) local += S.ucnt[u0 + j];
+                uint64_t ftotal;
+                uint64_t run = block_exclusive_scan<kRT>(local, s_warp, &ftotal);
+                for (uint32_t j = 0; j < per; j++) {
+                    if (u0 + j < nunit) {
+                        S.ufrag[u0 + j] = (uint32_t)run;
+                        run += S.ucnt[u0 + j];
+                    }
+                }
+                if (threadIdx.x == 0) s_ftotal = (uint32_t)ftotal;
+            }
+            __syncthreads();
+            const uint32_t ftotal = s_ftotal;
+
+            // ---- rounds: fragment offsets [base, base + F), in unit order,
+            // so that a pixel's fragments of earlier units are applied first
+            for (uint32_t base = 0; base < ftotal; base += (uint32_t)F) {
+                if (threadIdx.x == 0) {
+                    s_nfrag = 0;
+                    s_conflict = 0;
+                }
+                __syncthreads();
+                const uint32_t rend = min(base + (uint32_t)F, ftotal);
+                for (uint32_t w0 = base + threadIdx.x * kWin; w0 < rend; w0 += blockDim.x * kWin) {
+                    const uint32_t w1 = min(w0 + (uint32_t)kWin, rend);
+                    // the unit holding offset w0: the last one starting at or before it
+                    uint32_t lo = 0, hi = nunit - 1;
+                    while (lo < hi) {
+                        const uint32_t mid = (lo + hi + 1) >> 1;
+                        if (S.ufrag[mid] <= w0) lo = mid;
+                        else hi = mid - 1;
+                    }
+                    uint32_t u = lo, off = w0;
+                    while (off < w1) {
+                        const uint32_t fu = S.ufrag[u], cnt = S.ucnt[u];
+                        const uint32_t o = off - fu;
+                        const uint32_t len = min(w1 - off, fu + cnt - off);
+                        const uint32_t pp = S.cprim[S.uslot[u]];
+                        const RPrim& R = P.prims[pp];
+                        double e0 = S.uw0[u], e1 = S.uw1[u], e2 = S.uw2[u];
+                        if (o) {  // the edge values o steps further along the row
+                            e0 = repeat_add(e0, R.a0, o);
+                            e1 = repeat_add(e1, R.a1, o);
+                            e2 = repeat_add(e2, R.a2, o);
+                        }
+                        const int32_t pix = (S.urow[u] - B.r0) * I.W + S.ux[u] + (int32_t)o;
+                        emit_segment(R, I, B, S, pix, (int32_t)len, e0, e1, e2, u, &s_nfrag, &s_conflict);
+                        vis += len;
+                        off += len;
+                        u++;
+                    }
+                }
+                __syncthreads();
                 const uint32_t nfrag = s_nfrag;
                 if (threadIdx.x == 0) shd += nfrag;
                 for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) shade_fragment<PREC>(P, I, S, f);
                 __syncthreads();
                 resolve_chunk(P, I, B, S, nfrag, (s_conflict & 1u) != 0, upd);
                 __syncthreads();
-                const int more = big ? __syncthreads_or(threadIdx.x < nunit && !wk.done) : 0;
-                if (!more) break;
             }
-            const bool redo = (s_conflict & 2u) != 0;
-            __syncthreads();
-            if (redo && !box_bound) {  // one redo per chunk, with bounds that cannot fail
-                box_bound = true;
-                continue;
-            }
-            if (redo && threadIdx.x == 0) atomicOr(P.status, ST_RASTER_INTERNAL);
-            box_bound = false;
             k += nprim;
         }
         for (int j = threadIdx.x; j < npx; j += blockDim.x) I.depth[B.i0 + j] = S.depth[j];

@@ -36,6 +36,35 @@ def _dot(a, b):
     return a[..., 0] * b[..., 0] + a[..., 1] * b[..., 1] + a[..., 2] * b[..., 2]
 
 
+def group_rows(rows):
+    """Group id of each row of an (n, 3) float64 array: rows with equal bit
+    patterns share an id (ids are 0..groups-1). The rows' 64-bit mixed hash is
+    grouped first; the grouping is then checked row by row against each
+    group's first row, and an exact sort of the rows replaces it if two
+    different rows ever share a hash."""
+    rows = np.ascontiguousarray(rows, dtype=np.float64)
+    b = rows.view(np.uint64).reshape(-1, 3)
+
+    def fmix(z):  # splitmix64 finaliser
+        z = z ^ (z >> np.uint64(30))
+        z = z * np.uint64(0xBF58476D1CE4E5B9)
+        z = z ^ (z >> np.uint64(27))
+        z = z * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+    with np.errstate(over="ignore"):
+        h = fmix(b[:, 0] + np.uint64(0x9E3779B97F4A7C15))
+        h = fmix(h ^ fmix(b[:, 1] + np.uint64(0x632BE59BD9B4E019)))
+        h = fmix(h ^ fmix(b[:, 2] + np.uint64(0x2545F4914F6CDD1D)))
+    _, first, inv = np.unique(h, return_index=True, return_inverse=True)
+    inv = inv.ravel()
+    if np.array_equal(b, b[first[inv]]):
+        return inv
+    keys = rows.view(np.dtype((np.void, 24))).ravel()
+    _, inv = np.unique(keys, return_inverse=True)
+    return inv.ravel()
+
+
 def face_normals(tri_pos):
     """Triangle.Normal (triangle.go:33-37) for (T,3,3) positions."""
     e1 = tri_pos[:, 1] - tri_pos[:, 0]
@@ -264,9 +293,7 @@ class Mesh:
         order lists corner indices grouped by key, each group in corner
         (triangle, then V1..V3) order."""
         p = self.tri_pos.reshape(-1, 3) + 0.0  # -0 -> +0
-        keys = np.ascontiguousarray(p).view(np.dtype((np.void, 24))).ravel()
-        _, inv = np.unique(keys, return_inverse=True)
-        inv = inv.ravel()
+        inv = group_rows(p)
         order = np.argsort(inv, kind="stable")
         counts = np.bincount(inv)
         starts = np.concatenate([[0], np.cumsum(counts)[:-1]])

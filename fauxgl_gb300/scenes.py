@@ -17,7 +17,7 @@ import math
 import numpy as np
 
 from .geom import HexColor, LookAt, Perspective, Radians, V, Vector
-from .mesh import Mesh, _normalize, face_normals
+from .mesh import Mesh, _normalize, face_normals, group_rows
 from .shapes import cylinder_segments, sphere_positions
 
 EYE = V(-3, 1, -0.75)
@@ -80,13 +80,16 @@ def displace(pos, seed, octaves=8, amplitude=0.15, base_frequency=3.0):
         d = rng.unit_vector()
         mag = (2.0 ** k) * base_frequency
         waves.append((d[0] * mag, d[1] * mag, d[2] * mag, 2 * math.pi * rng.uniform(), amplitude * 2.0 ** -k))
-    flat = pos.reshape(-1, 3)
-    uniq, inv = np.unique(flat, axis=0, return_inverse=True)
+    flat = np.ascontiguousarray(pos.reshape(-1, 3), dtype=np.float64)
+    inv = group_rows(flat)
+    first = np.zeros(int(inv.max()) + 1 if inv.size else 0, dtype=np.int64)
+    first[inv[::-1]] = np.arange(inv.size)[::-1]  # each group's first row
+    uniq = flat[first]
     r = np.ones(uniq.shape[0])
     for kx, ky, kz, ph, amp in waves:
         r = r + amp * np.sin(kx * uniq[:, 0] + ky * uniq[:, 1] + kz * uniq[:, 2] + ph)
     out = uniq * r[:, None]
-    return out[inv.ravel()].reshape(pos.shape)
+    return out[inv].reshape(pos.shape)
 
 
 def displaced_sphere(detail=8, seed=1, smooth_degrees=30.0):
