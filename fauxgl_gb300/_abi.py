@@ -115,6 +115,8 @@ class FgcBatchTuning(ctypes.Structure):
         ("prims_per_bin_block", ctypes.c_int32),
         ("fragment_cap", ctypes.c_int32),
         ("use_graph", ctypes.c_int32),
+        ("window", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
 

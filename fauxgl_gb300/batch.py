@@ -107,8 +107,10 @@ class Batch:
         _abi.check(self._lib.fgc_batch_get_tuning(self.handle, ctypes.byref(t)))
         return {name: int(getattr(t, name)) for name, _ in _abi.FgcBatchTuning._fields_}
 
-    def SetTuning(self, band_pixels=4096, prims_per_bin_block=4096, fragment_cap=1024, use_graph=0):
-        t = _abi.FgcBatchTuning(int(band_pixels), int(prims_per_bin_block), int(fragment_cap), int(use_graph))
+    def SetTuning(self, band_pixels=4096, prims_per_bin_block=4096, fragment_cap=1024, use_graph=0, window=8,
+                  reserved=0):
+        t = _abi.FgcBatchTuning(int(band_pixels), int(prims_per_bin_block), int(fragment_cap), int(use_graph),
+                                int(window), 0)
         _abi.check(self._lib.fgc_batch_set_tuning(self.handle, ctypes.byref(t)))
 
     def Autotune(self, repeats=2):

@@ -75,6 +75,17 @@ int fill_views(const fgc_state* st, const fgc_shader* sh, StateView& sv, ShaderV
     memcpy(shv.diffuse, sh->diffuse_color, sizeof(shv.diffuse));
     memcpy(shv.specular, sh->specular_color, sizeof(shv.specular));
     shv.power = sh->specular_power;
+    for (int k = 0; k < 4; k++) {
+        shv.color32[k] = (float)shv.color[k];
+        shv.ambient32[k] = (float)shv.ambient[k];
+        shv.diffuse32[k] = (float)shv.diffuse[k];
+        shv.specular32[k] = (float)shv.specular[k];
+    }
+    for (int k = 0; k < 3; k++) {
+        shv.light32[k] = (float)shv.light[k];
+        shv.eye32[k] = (float)shv.eye[k];
+    }
+    shv.power32 = (float)shv.power;
     shv.object_is_discard = (sh->color[0] == 0 && sh->color[1] == 0 && sh->color[2] == 0 && sh->color[3] == 0);
     if (sh->texture) {
         shv.has_texture = 1;

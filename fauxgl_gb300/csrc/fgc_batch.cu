@@ -287,13 +287,15 @@ int fgc_batch_set_stream(fgc_batch* b, void* cuda_stream) {
 
 int fgc_batch_set_tuning(fgc_batch* b, const fgc_batch_tuning* t) {
     if (!b || !t) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
-    if (t->band_pixels < 1 || t->prims_per_bin_block < 1 || t->fragment_cap < 256)
+    if (t->band_pixels < 1 || t->prims_per_bin_block < 1 || t->fragment_cap < 256 || t->window < 0 ||
+        t->window > 256)
         return fail(FGC_ERR_INVALID_ARGUMENT, "tuning values out of range");
     std::lock_guard<std::mutex> lock(b->mu);
     if (b->inflight) return fail(FGC_ERR_BUSY, "the batch has a submission in flight");
     b->tuning.band_pixels = t->band_pixels;
     b->tuning.prims_per_bin_block = t->prims_per_bin_block;
     b->tuning.frag_cap = t->fragment_cap;
+    b->tuning.window = t->window ? t->window : 8;
     b->use_graph = t->use_graph != 0;
     return FGC_OK;
 }
@@ -304,6 +306,8 @@ int fgc_batch_get_tuning(const fgc_batch* b, fgc_batch_tuning* t) {
     t->prims_per_bin_block = (int32_t)b->tuning.prims_per_bin_block;
     t->fragment_cap = b->tuning.frag_cap;
     t->use_graph = b->use_graph ? 1 : 0;
+    t->window = b->tuning.window;
+    t->reserved = 0;
     return FGC_OK;
 }
 
@@ -375,10 +379,11 @@ int fgc_batch_autotune(fgc_batch* b, const fgc_batch_item* items, uint64_t n, in
         *ms = t[t.size() / 2];
         return FGC_OK;
     };
-    // coordinate descent over the three shapes, one sweep in this order
+    // coordinate descent over the four shapes, one sweep in this order
     const int64_t bands[] = {2048, 4096, 8192};
     const int64_t blocks[] = {2048, 4096, 8192, 16384};
     const int frags[] = {512, 768, 1024};
+    const int windows[] = {4, 8, 16, 32};
     PassTuning cur = b->tuning;
     double cur_ms = 0;
     int rc = measure(&cur_ms);
@@ -417,12 +422,20 @@ int fgc_batch_autotune(fgc_batch* b, const fgc_batch_item* items, uint64_t n, in
         c.frag_cap = v;
         if ((rc = try_one(c))) return rc;
     }
+    for (int v : windows) {
+        if (v == cur.window) continue;
+        PassTuning c = cur;
+        c.window = v;
+        if ((rc = try_one(c))) return rc;
+    }
     b->tuning = cur;
     if (best) {
         best->band_pixels = (int32_t)cur.band_pixels;
         best->prims_per_bin_block = (int32_t)cur.prims_per_bin_block;
         best->fragment_cap = cur.frag_cap;
         best->use_graph = b->use_graph ? 1 : 0;
+        best->window = cur.window;
+        best->reserved = 0;
     }
     return FGC_OK;
 }

@@ -81,9 +81,13 @@ struct __align__(16) VScreen { // Screen.MulPosition(ndc) and 1/W
 struct __align__(16) APosNrm64 { double px, py, pz, nx, ny, nz; };
 struct __align__(16) APosNrm32 { float px, py, pz, nx, ny, nz; };
 
-// A vertex of the clip pool (an InterpolateVertexes result).
+// A vertex of the clip pool (an InterpolateVertexes result), and its FP32
+// copy for the mixed form.
 struct __align__(16) PoolVertex {
     double px, py, pz, nx, ny, nz, tu, tv, cr, cg, cb, ca;
+};
+struct __align__(16) PoolVertex32 {
+    float px, py, pz, nx, ny, nz, tu, tv, cr, cg, cb, ca;
 };
 
 // Device view of a mesh.
@@ -120,6 +124,13 @@ struct ShaderView {
     double ambient[4], diffuse[4], specular[4];
     double power;
     TexView tex;
+    // the same parameters in FP32 for the mixed form (converted once on the
+    // host: a conversion from FP64 runs on the FP64 pipe)
+    float color32[4];
+    float light32[3];
+    float eye32[3];
+    float ambient32[4], diffuse32[4], specular32[4];
+    float power32;
 };
 
 struct StateView {
@@ -217,6 +228,25 @@ __device__ __forceinline__ bool dlt1(double x) {
 __device__ __forceinline__ bool dgt0(double x) {
     const unsigned long long b = dbits(x);
     return (b >> 63) == 0 && b != 0 && !bnan(b);
+}
+// x > y and x <= y exactly as IEEE compares (NaN: false; -0 == +0).
+__device__ __forceinline__ unsigned long long okey0(unsigned long long b) {
+    return okey((b & kAbsMask) ? b : 0ull);
+}
+__device__ __forceinline__ bool dgt_i(double x, double y) {
+    const unsigned long long bx = dbits(x), by = dbits(y);
+    if (bnan(bx) || bnan(by)) return false;
+    return okey0(bx) > okey0(by);
+}
+__device__ __forceinline__ bool dle_i(double x, double y) {
+    const unsigned long long bx = dbits(x), by = dbits(y);
+    if (bnan(bx) || bnan(by)) return false;
+    return okey0(bx) <= okey0(by);
+}
+// z + bias, skipping the add for a bias of +0: z + (+0) is z, or +0 for
+// z = -0, and every use compares it, where -0 and +0 are equal.
+__device__ __forceinline__ double add_bias(double z, double bias, bool bias_zero) {
+    return bias_zero ? z : __dadd_rn(z, bias);
 }
 
 // uint8(Clamp(c, 0, 1) * 255) (color.go:56-63): the clamp and the truncation

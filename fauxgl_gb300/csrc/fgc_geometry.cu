@@ -98,6 +98,7 @@ __device__ void make_prim(const GeomParams& P, uint64_t slot, D3 s0, D3 s1, D3 s
     R.elem = elem;
     P.prims[slot] = R;
     P.pbox[slot] = PBox{(int32_t)x0, (int32_t)x1, (int32_t)y0, (int32_t)y1};
+    P.rf[slot] = make_float4((float)r0, (float)r1, (float)r2, 0.0f);
     // A row's covered pixel centres lie on one horizontal chord of the
     // triangle, so a row holds at most (widest chord) + 1 of them; +3 more
     // cover rounding at both ends and in this estimate. The raster stage
@@ -430,9 +431,15 @@ __global__ void __launch_bounds__(128) clip_triangles_kernel(GeomParams P) {
             uint32_t pref[3];
             for (int c = 0; c < 3; c++) {
                 uint32_t pi = e * 21 + sub * 3 + c;
-                if (mask)
+                if (mask) {
                     P.pool[pi] = PoolVertex{v[c].pos.x, v[c].pos.y, v[c].pos.z, v[c].nrm.x, v[c].nrm.y, v[c].nrm.z,
                                             v[c].tu, v[c].tv, v[c].col.x, v[c].col.y, v[c].col.z, v[c].col.w};
+                    if (I.st.precision == FGC_PRECISION_MIXED)
+                        P.pool32[pi] = PoolVertex32{(float)v[c].pos.x, (float)v[c].pos.y, (float)v[c].pos.z,
+                                                    (float)v[c].nrm.x, (float)v[c].nrm.y, (float)v[c].nrm.z,
+                                                    (float)v[c].tu, (float)v[c].tv, (float)v[c].col.x,
+                                                    (float)v[c].col.y, (float)v[c].col.z, (float)v[c].col.w};
+                }
                 pref[c] = kPoolFlag | pi;
             }
             int i0 = 0, i2 = 2;

@@ -164,6 +164,7 @@ struct PassTuning {
     int64_t band_pixels = 4096;         // pixels per band, rounded to whole rows
     int64_t prims_per_bin_block = 4096; // raster primitives per binning block
     int frag_cap = 1024;                // upper bound of the raster fragment buffer
+    int window = 8;                     // raster fragment offsets per thread and round (wide primitives)
 };
 
 // One draw of a pass, as the host describes it.
@@ -187,9 +188,11 @@ struct PassScratch {
     DevBuf<uint8_t> vout;
     DevBuf<RPrim> prims;
     DevBuf<PBox> pbox;
+    DevBuf<float4> rf;
     DevBuf<uint32_t> pspan;
     DevBuf<ClipEntry> clip_list, lclip_list;
     DevBuf<PoolVertex> pool;
+    DevBuf<PoolVertex32> pool32;
     DevBuf<uint32_t> mat, off, bins;
     DevBuf<unsigned long long> tiles;
     DevBuf<unsigned char> table;   // item views + lookup starts + per-draw results + counters + status

@@ -108,6 +108,7 @@ struct GeomParams {
     const uint8_t* vout;
     RPrim* prims;
     PBox* pbox;
+    float4* rf;                 // per primitive: 1/W of its vertices in FP32 (mixed-form shading)
     uint32_t* pspan;            // per primitive: bound on covered pixels in one row
     uint64_t prim_cap;          // slots available in prims / pbox
     ClipEntry* clip_list;       // clipped triangles
@@ -116,6 +117,7 @@ struct GeomParams {
     ClipEntry* lclip_list;      // clipped lines (capacity: all lines of the pass)
     uint32_t* lclip_count;
     PoolVertex* pool;           // 21 per clip_list entry
+    PoolVertex32* pool32;       // FP32 copies (draws in the mixed form)
     unsigned long long* prim_total;
     Lookback lb;
     unsigned int* status;
@@ -158,7 +160,10 @@ struct RasterParams {
     const unsigned long long* pair_total;
     int32_t F;                  // fragment buffer capacity
     int32_t Lmax;               // largest band of the pass (depth staging)
+    int32_t win;                // fragment offsets a thread walks per round (wide primitives)
     const PoolVertex* pool;
+    const PoolVertex32* pool32;
+    const float4* rf;
     unsigned int* band_counter;
     unsigned int* status;
     double* dbg;                // debug scratch: gridDim * F * 4 doubles, or null

@@ -279,9 +279,11 @@ int plan_submission(PassScratch& S, const DevLimits& D, const PassTuning& T, con
     FGC_CUDA(S.vout.ensure(need_vert));
     FGC_CUDA(S.prims.ensure(need_prims));
     FGC_CUDA(S.pbox.ensure(need_prims));
+    FGC_CUDA(S.rf.ensure(need_prims));
     FGC_CUDA(S.pspan.ensure(need_prims));
     FGC_CUDA(S.clip_list.ensure(S.clip_cap));
     FGC_CUDA(S.pool.ensure((size_t)S.clip_cap * 21));
+    FGC_CUDA(S.pool32.ensure((size_t)S.clip_cap * 21));
     FGC_CUDA(S.lclip_list.ensure(need_lines));
     FGC_CUDA(S.mat.ensure(need_mat));
     FGC_CUDA(S.off.ensure(need_mat));
@@ -396,6 +398,7 @@ int issue_submission(PassScratch& S, cudaStream_t stream, const DevLimits& D, co
         gp.vout = S.vout.p;
         gp.prims = S.prims.p;
         gp.pbox = S.pbox.p;
+        gp.rf = S.rf.p;
         gp.pspan = S.pspan.p;
         gp.prim_cap = prim_cap;
         gp.clip_list = S.clip_list.p;
@@ -404,6 +407,7 @@ int issue_submission(PassScratch& S, cudaStream_t stream, const DevLimits& D, co
         gp.lclip_list = S.lclip_list.p;
         gp.lclip_count = &dc->lclip_count;
         gp.pool = S.pool.p;
+        gp.pool32 = S.pool32.p;
         gp.prim_total = &dc->prim_total;
         gp.lb = Lookback{t_setup, &dc->tick_setup, status, &dc->prim_total};
         gp.status = status;
@@ -474,7 +478,10 @@ int issue_submission(PassScratch& S, cudaStream_t stream, const DevLimits& D, co
         rp.pair_total = &dc->pair_total;
         rp.F = P.F;
         rp.Lmax = P.Lmax;
+        rp.win = std::max(1, std::min(T.window, 256));
         rp.pool = S.pool.p;
+        rp.pool32 = S.pool32.p;
+        rp.rf = S.rf.p;
         rp.band_counter = &dc->band_counter;
         rp.status = status;
         rp.dbg = P.debug_shaded ? S.dbg.p : nullptr;

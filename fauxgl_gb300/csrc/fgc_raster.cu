@@ -15,7 +15,7 @@
 //             (row start, skip-ahead d, per-pixel adds, inside test, break).
 //             Wide ones: one thread per unit finds the row's covered interval
 //             and its first edge values (exact jumps through the serial sums,
-//             fgc_fpjump.cuh), then all threads walk windows of kWin pixels.
+//             fgc_fpjump.cuh), then all threads walk windows of P.win pixels.
 //             An early depth test against the band's current depth drops
 //             fragments that cannot update (only when depth can only
 //             decrease during the draw).
@@ -222,9 +222,9 @@ __device__ __forceinline__ float interpf(float a, float b, float c, float wx, fl
 
 __device__ __forceinline__ void fetch_pn32(const RasterParams& P, const MeshView& M, uint32_t v, F3& pos, F3& nrm) {
     if (v & kPoolFlag) {
-        const PoolVertex& q = P.pool[v & ~kPoolFlag];
-        pos = F3{(float)q.px, (float)q.py, (float)q.pz};
-        nrm = F3{(float)q.nx, (float)q.ny, (float)q.nz};
+        const PoolVertex32& q = P.pool32[v & ~kPoolFlag];
+        pos = F3{q.px, q.py, q.pz};
+        nrm = F3{q.nx, q.ny, q.nz};
     } else {
         APosNrm32 a = M.pn32[v];
         pos = F3{a.px, a.py, a.pz};
@@ -267,12 +267,12 @@ __device__ float powf_int_or_general(float x, float p) {
     return powf(x, p);
 }
 
-__device__ float4 shade32(const RasterParams& P, const ItemView& I, const RPrim& R, double b0, double b1, double b2) {
+__device__ float4 shade32(const RasterParams& P, const ItemView& I, const RPrim& R, float4 rf, double b0, double b1,
+                         double b2) {
     const ShaderView& S = I.sh;
     const MeshView& M = I.mesh;
-    if (S.kind == FGC_SHADER_SOLID_COLOR)
-        return make_float4((float)S.color[0], (float)S.color[1], (float)S.color[2], (float)S.color[3]);
-    float wx = (float)b0 * (float)R.r0, wy = (float)b1 * (float)R.r1, wz = (float)b2 * (float)R.r2;
+    if (S.kind == FGC_SHADER_SOLID_COLOR) return make_float4(S.color32[0], S.color32[1], S.color32[2], S.color32[3]);
+    float wx = (float)b0 * rf.x, wy = (float)b1 * rf.y, wz = (float)b2 * rf.z;
     float ww = 1.0f / (wx + wy + wz);
     float4 color;
     bool have_color = false;
@@ -281,9 +281,9 @@ __device__ float4 shade32(const RasterParams& P, const ItemView& I, const RPrim&
         uint32_t vr[3] = {R.v0, R.v1, R.v2};
         for (int k = 0; k < 3; k++) {
             if (vr[k] & kPoolFlag) {
-                const PoolVertex& q = P.pool[vr[k] & ~kPoolFlag];
-                u[k] = (float)q.tu;
-                v[k] = (float)q.tv;
+                const PoolVertex32& q = P.pool32[vr[k] & ~kPoolFlag];
+                u[k] = q.tu;
+                v[k] = q.tv;
             } else if (M.tex32) {
                 u[k] = M.tex32[2 * (uint64_t)vr[k]];
                 v[k] = M.tex32[2 * (uint64_t)vr[k] + 1];
@@ -310,8 +310,8 @@ __device__ float4 shade32(const RasterParams& P, const ItemView& I, const RPrim&
             float c[3][4];
             for (int k = 0; k < 3; k++) {
                 if (vr[k] & kPoolFlag) {
-                    const PoolVertex& q = P.pool[vr[k] & ~kPoolFlag];
-                    c[k][0] = (float)q.cr; c[k][1] = (float)q.cg; c[k][2] = (float)q.cb; c[k][3] = (float)q.ca;
+                    const PoolVertex32& q = P.pool32[vr[k] & ~kPoolFlag];
+                    c[k][0] = q.cr; c[k][1] = q.cg; c[k][2] = q.cb; c[k][3] = q.ca;
                 } else if (M.col32) {
                     for (int j = 0; j < 4; j++) c[k][j] = M.col32[4 * (uint64_t)vr[k] + j];
                 } else {
@@ -323,27 +323,27 @@ __device__ float4 shade32(const RasterParams& P, const ItemView& I, const RPrim&
                                 interpf(c[0][2], c[1][2], c[2][2], wx, wy, wz, ww),
                                 interpf(c[0][3], c[1][3], c[2][3], wx, wy, wz, ww));
         } else {
-            color = make_float4((float)S.color[0], (float)S.color[1], (float)S.color[2], (float)S.color[3]);
+            color = make_float4(S.color32[0], S.color32[1], S.color32[2], S.color32[3]);
         }
     }
-    F3 L = F3{(float)S.light[0], (float)S.light[1], (float)S.light[2]};
-    float lr = (float)S.ambient[0], lg = (float)S.ambient[1], lb = (float)S.ambient[2];
+    F3 L = F3{S.light32[0], S.light32[1], S.light32[2]};
+    float lr = S.ambient32[0], lg = S.ambient32[1], lb = S.ambient32[2];
     float nl = dotf3(nrm, L);
     float diffuse = (nl > 0.0f) ? nl : ((nl != nl) ? nl : 0.0f);
-    lr = __fmaf_rn((float)S.diffuse[0], diffuse, lr);
-    lg = __fmaf_rn((float)S.diffuse[1], diffuse, lg);
-    lb = __fmaf_rn((float)S.diffuse[2], diffuse, lb);
+    lr = __fmaf_rn(S.diffuse32[0], diffuse, lr);
+    lg = __fmaf_rn(S.diffuse32[1], diffuse, lg);
+    lb = __fmaf_rn(S.diffuse32[2], diffuse, lb);
     if (diffuse > 0 && S.power > 0) {
-        F3 cam = normf3(F3{(float)S.eye[0] - pos.x, (float)S.eye[1] - pos.y, (float)S.eye[2] - pos.z});
+        F3 cam = normf3(F3{S.eye32[0] - pos.x, S.eye32[1] - pos.y, S.eye32[2] - pos.z});
         F3 negl = F3{-L.x, -L.y, -L.z};
         float k = 2.0f * dotf3(nrm, negl);
         F3 refl = F3{negl.x - nrm.x * k, negl.y - nrm.y * k, negl.z - nrm.z * k};
         float sp = dotf3(cam, refl);
         if (sp > 0) {
-            sp = powf_int_or_general(sp, (float)S.power);
-            lr = __fmaf_rn((float)S.specular[0], sp, lr);
-            lg = __fmaf_rn((float)S.specular[1], sp, lg);
-            lb = __fmaf_rn((float)S.specular[2], sp, lb);
+            sp = powf_int_or_general(sp, S.power32);
+            lr = __fmaf_rn(S.specular32[0], sp, lr);
+            lg = __fmaf_rn(S.specular32[1], sp, lg);
+            lb = __fmaf_rn(S.specular32[2], sp, lb);
         }
     }
     return make_float4(fminf(color.x * lr, 1.0f), fminf(color.y * lg, 1.0f), fminf(color.z * lb, 1.0f), color.w);
@@ -368,11 +368,10 @@ __device__ __forceinline__ uint32_t u8_of_unit_f32(float c) {
 //            jumps for long ones) and the edge values at its first pixel in
 //            the band;
 //   windows  the chunk's covered pixels, numbered in unit order, are dealt
-//            out kWin at a time; a window that starts inside a row starts
+//            out P.win at a time; a window that starts inside a row starts
 //            from an exact jump (repeat_add) and walks on from there.
 // Every value is the one the serial walk would have had: the same adds in
 // the same order, only not all of them executed one after the other.
-constexpr int kWin = 8;          // fragment offsets one thread walks in a round
 constexpr int kNarrow = 32;      // boxes at most this wide are walked row by row
 constexpr int kShortRow = 40;    // rows of at most this many steps are walked plainly
 
@@ -577,6 +576,7 @@ __device__ __forceinline__ uint32_t walk_row(const RPrim& R, const PBox& bx, int
     double w2 = __dadd_rn(w02, __dmul_rn(R.a2, d));
     const int32_t rel = (y - B.r0) * I.W;
     const double bias = I.st.depth_bias;
+    const bool bias_zero = dbits(bias) == 0;
     const double ra = R.ra;
     const RaSign rs = ra_sign(ra);
     uint32_t total = 0;
@@ -602,7 +602,7 @@ __device__ __forceinline__ uint32_t walk_row(const RPrim& R, const PBox& bx, int
         const double b1 = __dmul_rn(c1, ra);
         const double b2 = __dmul_rn(c2, ra);
         const double z = __dadd_rn(__dadd_rn(__dmul_rn(b0, R.z0), __dmul_rn(b1, R.z1)), __dmul_rn(b2, R.z2));
-        if (B.early && __dadd_rn(z, bias) > S.depth[pix]) continue;
+        if (B.early && dgt_i(add_bias(z, bias, bias_zero), S.depth[pix])) continue;
         const uint32_t slot = atomicAdd(s_nfrag, 1u);
         if (slot >= (uint32_t)P.F) {
             atomicOr(s_conflict, 2u);
@@ -633,6 +633,7 @@ __device__ __forceinline__ void emit_segment(const RPrim& R, const ItemView& I, 
                                              int32_t pix, int32_t len, double w0, double w1, double w2, uint32_t unit,
                                              uint32_t* s_nfrag, uint32_t* s_conflict) {
     const double bias = I.st.depth_bias;
+    const bool bias_zero = dbits(bias) == 0;
     const double ra = R.ra;
     for (int32_t i = 0; i < len; i++, pix++) {
         const double b0 = __dmul_rn(w0, ra);
@@ -644,7 +645,7 @@ __device__ __forceinline__ void emit_segment(const RPrim& R, const ItemView& I, 
             w2 = __dadd_rn(w2, R.a2);
         }
         const double z = __dadd_rn(__dadd_rn(__dmul_rn(b0, R.z0), __dmul_rn(b1, R.z1)), __dmul_rn(b2, R.z2));
-        if (B.early && __dadd_rn(z, bias) > S.depth[pix]) continue;
+        if (B.early && dgt_i(add_bias(z, bias, bias_zero), S.depth[pix])) continue;
         const uint32_t slot = atomicAdd(s_nfrag, 1u);  // below F: the round was sized for every pixel
         S.fb0[slot] = b0;
         S.fb1[slot] = b1;
@@ -673,8 +674,8 @@ __device__ __forceinline__ void apply_fragment(const RasterParams& P, const Item
     const int pix = (int)(key >> 16);
     const int unit = (int)(key & 0xffff);
     const double z = S.fz[f];
-    const double bz = __dadd_rn(z, I.st.depth_bias);
-    if (!I.st.read_depth || bz <= S.depth[pix]) {
+    const double bz = add_bias(z, I.st.depth_bias, dbits(I.st.depth_bias) == 0);
+    if (!I.st.read_depth || dle_i(bz, S.depth[pix])) {
         updated++;
         if (I.st.write_depth) S.depth[pix] = z;
         if (I.st.write_color) {
@@ -720,7 +721,7 @@ __device__ __forceinline__ void shade_fragment(const RasterParams& P, const Item
         if (I.st.alpha_blend && dlt1(col.w)) fl |= kFragBlend;
         packed = nrgba_pack_i(col.x, col.y, col.z, col.w);
     } else {
-        float4 col = shade32(P, I, R, b0, b1, b2);
+        float4 col = shade32(P, I, R, P.rf[S.cprim[S.uslot[unit]]], b0, b1, b2);
         c[0] = col.x; c[1] = col.y; c[2] = col.z; c[3] = col.w;
         if (col.x == 0 && col.y == 0 && col.z == 0 && col.w == 0) fl |= kFragDiscard;
         if (I.st.alpha_blend && col.w < 1) fl |= kFragBlend;
@@ -1037,8 +1038,9 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
                 }
                 __syncthreads();
                 const uint32_t rend = min(base + (uint32_t)F, ftotal);
-                for (uint32_t w0 = base + threadIdx.x * kWin; w0 < rend; w0 += blockDim.x * kWin) {
-                    const uint32_t w1 = min(w0 + (uint32_t)kWin, rend);
+                const uint32_t win = (uint32_t)P.win;  // fragment offsets one thread walks
+                for (uint32_t w0 = base + threadIdx.x * win; w0 < rend; w0 += blockDim.x * win) {
+                    const uint32_t w1 = min(w0 + win, rend);
                     // the unit holding offset w0: the last one starting at or before it
                     uint32_t lo = 0, hi = nunit - 1;
                     while (lo < hi) {

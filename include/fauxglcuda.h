@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define FGC_ABI_VERSION 2
+#define FGC_ABI_VERSION 3
 
 typedef enum fgc_status {
     FGC_OK = 0,
@@ -285,6 +285,8 @@ typedef struct fgc_batch_tuning {
     int32_t prims_per_bin_block;  /* primitives per binning block (default 4096)           */
     int32_t fragment_cap;         /* fragment buffer of a raster CTA (default 1024)        */
     int32_t use_graph;            /* 1: issue each submission as a CUDA graph              */
+    int32_t window;               /* raster pixels per thread and round for wide triangles (default 8) */
+    int32_t reserved;
 } fgc_batch_tuning;
 int fgc_batch_create(fgc_batch** out);
 int fgc_batch_destroy(fgc_batch* b);

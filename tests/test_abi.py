@@ -46,7 +46,7 @@ def test_struct_layouts_match_the_header(lib):
     assert ctypes.sizeof(_abi.FgcShader) == 8 + 8 * (16 + 4 + 3 + 3 + 4 + 4 + 4 + 1) + 8
     assert ctypes.sizeof(_abi.FgcRasterizeInfo) == 16
     assert ctypes.sizeof(_abi.FgcBatchItem) == 8 * 2 + 8 * 4 + 8 * 3 + 4 * 2
-    assert ctypes.sizeof(_abi.FgcBatchTuning) == 16
+    assert ctypes.sizeof(_abi.FgcBatchTuning) == 24
 
 
 def test_defaults_without_gpu(lib):

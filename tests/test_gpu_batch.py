@@ -256,7 +256,8 @@ def test_batch_overflow_is_rerun(gpu_lib):
         assert_same(ctx1, ctx)
 
 
-@pytest.mark.parametrize("tuning", [(2048, 2048, 512, 0), (8192, 16384, 768, 0), (4096, 4096, 1024, 1)])
+@pytest.mark.parametrize("tuning", [(2048, 2048, 512, 0, 4), (8192, 16384, 768, 0, 32), (4096, 4096, 1024, 1, 8),
+                                    (4096, 4096, 1024, 0, 1)])
 def test_batch_tuning_and_graph_do_not_change_results(gpu_lib, tuning):
     specs = make_specs(7, sizes=[(97, 61), (300, 170), (33, 200), (1024, 16)])
     alone = [draw_alone(sp) for sp in specs]
@@ -278,6 +279,7 @@ def test_batch_autotune(gpu_lib):
     t = _abi.FgcBatchTuning()
     _abi.check(b.lib.fgc_batch_autotune(b.h, items, len(specs), 1, ctypes.byref(t)))
     assert t.band_pixels in (2048, 4096, 8192) and t.fragment_cap in (512, 768, 1024)
+    assert t.window in (4, 8, 16, 32)
     cur = _abi.FgcBatchTuning()
     _abi.check(b.lib.fgc_batch_get_tuning(b.h, ctypes.byref(cur)))
     assert (cur.band_pixels, cur.prims_per_bin_block, cur.fragment_cap) == \
