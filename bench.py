@@ -71,9 +71,9 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per rate of the serving loop")
     ap.add_argument("--serve-max-requests", type=int, default=160, help="requests per rate at most")
     ap.add_argument("--serve-budget-gb", type=int, default=96, help="HBM budget of the serving loop")
-    ap.add_argument("--only", choices=["all", "plain", "ss16", "batch", "serve"], default="all",
-                    help="plain / ss16 / batch: time only the plain 1080p frame, the plain 16x supersampled "
-                         "frame or the thumbnail batch (for profiler runs)")
+    ap.add_argument("--only", choices=["all", "plain", "mixed", "ss16", "batch", "serve"], default="all",
+                    help="plain / mixed / ss16 / batch / serve: time only the plain or mixed 1080p frame, the plain "
+                         "16x supersampled frame, the thumbnail batch or the serving loop (for profiler runs)")
     return ap.parse_args()
 
 
@@ -601,6 +601,16 @@ def main():
         return 0
     if args.only == "batch":
         print(json.dumps({"batch": bench_batch(lib, args, torch)}), flush=True)
+        return 0
+    if args.only == "mixed":
+        f = Frame(lib, mesh_h, W, H, _abi.FGC_PRECISION_MIXED)
+        f.set_timing(True)
+        stage = [0.0] * 5
+        mixed_ms, _ = time_frames(f, args.steps, args.warmup, torch, barrier, stage)
+        print(json.dumps({"mixed_ms_per_frame": round(mixed_ms, 4), "value": round(1e3 / mixed_ms, 3),
+                          "stages_ms": {k: round(v / args.steps, 4) for k, v in zip(_abi.STAGE_NAMES, stage)},
+                          "work": work_dict(f.stats()), "steps": args.steps}), flush=True)
+        f.close()
         return 0
     if args.only == "serve":
         print(json.dumps({"serve": bench_serve(args, pool)}), flush=True)

@@ -208,11 +208,16 @@ constexpr int kRasterHeads = 2048;
 // this many rows.
 constexpr int kSpanUnits = 128;
 
+// Bin entries a raster thread examines per chunk, and the chunk's primitive
+// capacity (a chunk of narrow primitives may hold several units per thread).
+constexpr int kChunkPer = 1;
+constexpr int kChunkPrims = 256 * kChunkPer;
+
 // Dynamic shared memory of the raster kernel (layout in fgc_raster.cu), for
 // a fragment buffer of F: depth[L] f64, fragment b0/b1/b2/z[F] f64, span
 // edge values[kSpanUnits] 3 x f64, scratch 64 u64, fragment key/colour[F]
 // u32, unit slot/row[F] u32, span x/count/offset[kSpanUnits] u32, chunk
-// primitives[threads] u32, bucket list heads[kRasterHeads] u16, list
+// primitives[kChunkPrims] u32, bucket list heads[kRasterHeads] u16, list
 // links[F] u16, flags[F] u8. The colour buffer is not staged: the band's
 // pixels are read and written in global memory by the CTA that owns them.
 __host__ __device__ inline size_t raster_smem_bytes(int64_t L, int F, int threads) {
@@ -223,7 +228,7 @@ __host__ __device__ inline size_t raster_smem_bytes(int64_t L, int F, int thread
     b += 64 * 8;
     b += (size_t)F * 4 * 4;
     b += (size_t)kSpanUnits * 4 * 3;
-    b += (size_t)threads * 4;
+    b += (size_t)(threads > kChunkPrims ? threads : kChunkPrims) * 4;
     b += (size_t)kRasterHeads * 2;
     b += (size_t)F * 2;
     b += (size_t)F;

@@ -55,7 +55,7 @@ struct RasterSmem {
     int32_t* ux;     // [kSpanUnits] unit -> first covered in-band x
     uint32_t* ucnt;  // [kSpanUnits] unit -> covered in-band pixels
     uint32_t* ufrag; // [kSpanUnits] unit -> first fragment offset in the chunk
-    uint32_t* cprim; // [kRT] chunk slot -> primitive
+    uint32_t* cprim; // [kChunkPrims] chunk slot -> primitive
     unsigned short* head;  // [kHeads] per pixel bucket: last fragment of its list (0xFFFF: none)
     unsigned short* nxt;   // [F] per fragment: the previous fragment in its bucket
     uint8_t* fflag;  // [F] discard / blend flags
@@ -826,6 +826,56 @@ __device__ __forceinline__ void flush_counters(const RasterParams& P, uint32_t i
     tot = upd = vis = shd = 0;
 }
 
+// One bin entry as the chunk builder sees it: the primitive, its rows in the
+// band, a bound on its covered in-band pixels (rows x the widest chord, or x
+// the box width) and whether its box is narrow enough for the direct walk.
+struct ChunkEntry {
+    uint32_t p;
+    int32_t ylo, nrows;
+    uint32_t bound;  // capped at 2^31 - 1
+    bool narrow;
+};
+
+__device__ __forceinline__ ChunkEntry chunk_entry(const RasterParams& P, const ItemView& I, const BandCtx& B,
+                                                  uint64_t at, bool box_bound) {
+    ChunkEntry c;
+    c.p = P.bins[at];
+    const PBox bx = P.pbox[c.p];
+    rows_in_band(bx, I.W, B, c.ylo, c.nrows);
+    int64_t wid = (int64_t)bx.x1 - bx.x0 + 1;
+    c.narrow = wid <= kNarrow;
+    if (!box_bound && (int64_t)P.pspan[c.p] < wid) wid = P.pspan[c.p];
+    if (wid > B.npx) wid = B.npx;
+    if (wid < 0) wid = 0;
+    const uint64_t bound = (uint64_t)c.nrows * (uint64_t)wid;
+    c.bound = bound < 0x7FFFFFFFull ? (uint32_t)bound : 0x7FFFFFFFu;
+    return c;
+}
+
+// Fragment estimates are the bound scaled by ratio / kRatioOne.
+constexpr uint32_t kRatioOne = 256;
+constexpr uint32_t kRatioMin = 16;
+
+// The entry's share of a chunk's fragment budget F: its scaled bound in a
+// direct chunk (F + 1 for a wide primitive, which ends the chunk before it),
+// nothing in a span chunk (bounded by units instead).
+__device__ __forceinline__ uint64_t chunk_key(const ChunkEntry& c, bool direct, uint32_t ratio, int F) {
+    if (!direct) return 0;
+    if (!c.narrow) return (uint64_t)F + 1;
+    return ((uint64_t)c.bound * ratio + (kRatioOne - 1)) / kRatioOne;
+}
+
+// The ratio for the next chunk: twice the share of bounded pixels that
+// became fragments in this one, not below half the previous ratio.
+__device__ __forceinline__ uint32_t next_ratio(uint32_t prev, uint32_t nfrag, uint32_t bsum) {
+    if (bsum == 0) return prev;
+    uint64_t r = ((uint64_t)nfrag * 2 * kRatioOne + bsum - 1) / bsum;
+    if (r < prev / 2) r = prev / 2;
+    if (r < kRatioMin) r = kRatioMin;
+    if (r > kRatioOne) r = kRatioOne;
+    return (uint32_t)r;
+}
+
 template <int PREC>
 __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -849,12 +899,12 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
         S.ux = (int32_t*)q; q += (size_t)kSpanUnits * 4;
         S.ucnt = (uint32_t*)q; q += (size_t)kSpanUnits * 4;
         S.ufrag = (uint32_t*)q; q += (size_t)kSpanUnits * 4;
-        S.cprim = (uint32_t*)q; q += kRT * 4;
+        S.cprim = (uint32_t*)q; q += kChunkPrims * 4;
         S.head = (unsigned short*)q; q += (size_t)kRasterHeads * 2;
         S.nxt = (unsigned short*)q; q += (size_t)F * 2;
         S.fflag = (uint8_t*)q;
     }
-    __shared__ uint32_t s_band, s_item, s_nfrag, s_conflict, s_nprim, s_nunit, s_ftotal, s_mode;
+    __shared__ uint32_t s_band, s_item, s_nfrag, s_conflict, s_nprim, s_nunit, s_ftotal, s_mode, s_bsum, s_ratio;
     __shared__ uint64_t s_warp[kRT / 32 + 1];
     __shared__ ItemView s_iv;  // the draw of the current band
     const ItemView& I = s_iv;
@@ -882,6 +932,7 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
             const uint4* src = reinterpret_cast<const uint4*>(&P.items[item]);
             uint4* dst = reinterpret_cast<uint4*>(&s_iv);
             for (int j = threadIdx.x; j < (int)(sizeof(ItemView) / 16); j += blockDim.x) dst[j] = src[j];
+            if (threadIdx.x == 0) s_ratio = kRatioOne;
         }
         __syncthreads();
         const uint32_t band = gband - I.band0;
@@ -905,56 +956,71 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
         __syncthreads();
 
         uint64_t k = 0;
-        bool box_bound = false;  // size the next direct chunk by bounding boxes only
+        int level = 0;  // 0: estimated fragments, 1: widest-chord bound, 2: box bound
         while (k < bcount) {
-            // ---- chunk: a prefix of the remaining bin, at most one primitive
-            // per thread. Its first primitive picks how it is walked:
+            // ---- chunk: a prefix of the remaining bin; thread t examines
+            // entries k + kChunkPer*t + j. The first primitive picks how the
+            // chunk is walked:
             //   direct  narrow primitives, each row walked and recorded by one
-            //           thread as rasterize does; the prefix also keeps a bound
-            //           on its fragments within F (a row holds at most pspan,
-            //           its widest chord, covered pixels; box_bound falls back
-            //           to the box width after a chunk whose walk outgrew F)
+            //           thread as rasterize does, up to F units. The prefix
+            //           keeps an estimate of its fragments within F: at level
+            //           0 the bound (rows x widest chord) scaled by the share
+            //           of bounded pixels that became fragments in earlier
+            //           chunks (early depth rejection makes it small); a walk
+            //           that outgrows F is redone at level 1 with the bound
+            //           itself, then at level 2 with the box width
             //   spans   anything else, at most kSpanUnits units: spans, then
             //           windows of fragment offsets
-            uint32_t p = 0;
-            int32_t ylo = 0, nrows = 0;
-            uint64_t bound = 0;
-            bool narrow = true;
-            const bool valid = (k + threadIdx.x) < bcount;
-            if (valid) {
-                p = P.bins[bstart + k + threadIdx.x];
-                const PBox bx = P.pbox[p];
-                rows_in_band(bx, I.W, B, ylo, nrows);
-                int64_t wid = (int64_t)bx.x1 - bx.x0 + 1;
-                narrow = wid <= kNarrow;
-                if (!box_bound && (int64_t)P.pspan[p] < wid) wid = P.pspan[p];
-                if (wid > npx) wid = npx;
-                if (wid < 0) wid = 0;
-                bound = (uint64_t)nrows * (uint64_t)wid;
-            }
-            if (threadIdx.x == 0) s_mode = (narrow && bound <= (uint64_t)F) ? 1u : 0u;
-            __syncthreads();
-            const bool direct = s_mode != 0;
-            const uint64_t key = !direct ? 0 : (valid && narrow) ? bound : (uint64_t)F + 1;
-            uint64_t bagg, uagg;
-            const uint64_t bexcl = block_exclusive_scan<kRT>(key, s_warp, &bagg);
-            const uint64_t ubase = block_exclusive_scan<kRT>(valid ? (uint64_t)nrows : 0, s_warp, &uagg);
-            // a prefix, never empty (R <= kSpanUnits; a direct chunk's first
-            // bound <= F, and its units are at most its bound)
-            const uint64_t ucap = direct ? (uint64_t)F : (uint64_t)kSpanUnits;
-            const bool take = valid && ubase + (uint64_t)nrows <= ucap && bexcl + key <= (uint64_t)F;
+            const uint64_t e0 = k + (uint64_t)threadIdx.x * kChunkPer;
+            ChunkEntry ce[kChunkPer];
+#pragma unroll
+            for (int j = 0; j < kChunkPer; j++)
+                ce[j] = (e0 + j < bcount) ? chunk_entry(P, I, B, bstart + e0 + j, level == 2) : ChunkEntry{0, 0, 0, 0, true};
             if (threadIdx.x == 0) {
+                s_mode = (ce[0].narrow && ce[0].bound <= (uint32_t)F) ? 1u : 0u;
                 s_nprim = 0;
                 s_nunit = 0;
+                s_bsum = 0;
             }
             __syncthreads();
-            if (take) {
-                atomicAdd(&s_nprim, 1u);
-                atomicAdd(&s_nunit, (uint32_t)nrows);
-                S.cprim[threadIdx.x] = p;
-                for (int r = 0; r < nrows; r++) {
-                    S.uslot[ubase + r] = threadIdx.x;
-                    S.urow[ubase + r] = ylo + r;
+            const bool direct = s_mode != 0;
+            const uint32_t ratio = level == 0 ? s_ratio : kRatioOne;
+            // a direct chunk holds at most one unit per thread: a second pass
+            // over the units would double its first warps' walk
+            const uint64_t ucap = direct ? (uint64_t)min(F, kRT) : (uint64_t)kSpanUnits;
+            uint64_t tkey = 0, tun = 0;
+#pragma unroll
+            for (int j = 0; j < kChunkPer; j++) {
+                tkey += chunk_key(ce[j], direct, ratio, F);
+                tun += (uint64_t)ce[j].nrows;
+            }
+            uint64_t kagg, uagg;
+            uint64_t kr = block_exclusive_scan<kRT>(tkey, s_warp, &kagg);
+            uint64_t ur = block_exclusive_scan<kRT>(tun, s_warp, &uagg);
+            // the entries inside the prefix (never empty: R <= kSpanUnits, and
+            // a direct chunk's first estimate is at most its bound <= F)
+            {
+                const uint64_t ur0 = ur;
+                uint32_t took = 0, bsum = 0;
+#pragma unroll
+                for (int j = 0; j < kChunkPer; j++) {
+                    const uint64_t key = chunk_key(ce[j], direct, ratio, F);
+                    if (e0 + j >= bcount || ur + (uint64_t)ce[j].nrows > ucap || kr + key > (uint64_t)F) break;
+                    const uint32_t slot = threadIdx.x * kChunkPer + j;
+                    S.cprim[slot] = ce[j].p;
+                    for (int r = 0; r < ce[j].nrows; r++) {
+                        S.uslot[ur + r] = slot;
+                        S.urow[ur + r] = ce[j].ylo + r;
+                    }
+                    kr += key;
+                    ur += (uint64_t)ce[j].nrows;
+                    took++;
+                    bsum += min(ce[j].bound, (uint32_t)F);
+                }
+                if (took) {
+                    atomicAdd(&s_nprim, took);
+                    atomicAdd(&s_nunit, (uint32_t)(ur - ur0));
+                    atomicAdd(&s_bsum, bsum);
                 }
             }
             __syncthreads();
@@ -973,29 +1039,33 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
                 }
                 __syncthreads();
                 const bool redo = (s_conflict & 2u) != 0;
-                if (redo) {  // nothing was applied: empty the lists, redo with box bounds
+                if (redo) {  // nothing was applied: empty the lists, redo with a safer bound
                     const uint32_t nrec = min(s_nfrag, (uint32_t)F);
                     for (uint32_t f = threadIdx.x; f < nrec; f += blockDim.x)
                         S.head[bucket_of(S.fkey[f] >> 16)] = 0xFFFFu;
+                    if (threadIdx.x == 0) s_ratio = kRatioOne;
                 } else {
                     tot += tchunk;
                     const uint32_t nfrag = s_nfrag;
-                    if (threadIdx.x == 0) shd += nfrag;
+                    if (threadIdx.x == 0) {
+                        shd += nfrag;
+                        s_ratio = next_ratio(s_ratio, nfrag, s_bsum);
+                    }
                     for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) shade_fragment<PREC>(P, I, S, f);
                     __syncthreads();
                     resolve_chunk(P, I, B, S, nfrag, (s_conflict & 1u) != 0, upd);
                 }
                 __syncthreads();
-                if (redo && !box_bound) {
-                    box_bound = true;
+                if (redo && level < 2) {
+                    level++;
                     continue;
                 }
                 if (redo && threadIdx.x == 0) atomicOr(P.status, ST_RASTER_INTERNAL);
-                box_bound = false;
+                level = 0;
                 k += nprim;
                 continue;
             }
-            box_bound = false;
+            level = 0;
 
             // ---- spans: each unit's covered in-band pixels
             for (uint32_t u = threadIdx.x; u < nunit; u += blockDim.x) {
