@@ -393,6 +393,16 @@ __device__ __forceinline__ int edge_dir(double a, double ra) {
     return ((ab ^ rb) >> 63) ? -1 : 1;
 }
 
+// Whether edge k's test "w*ra < 0", once true along a row, stays true for
+// the rest of it: a and ra are not NaN and a is zero or of the opposite sign
+// to ra (w*ra never rises). A row whose walk meets an outside pixel failing
+// such an edge has no covered pixel after it, so the walk can end there.
+__device__ __forceinline__ bool stays_out(double a, double ra) {
+    const unsigned long long ab = dbits(a), rb = dbits(ra);
+    if (bnan(ab) || bnan(rb)) return false;
+    return (ab & kAbsMask) == 0 || ((ab ^ rb) >> 63) != 0;
+}
+
 // First step t in (lo, hi] at which edge k's test "w*ra < 0" becomes `want`,
 // or hi + 1. The test is monotone in t and differs from `want` at lo. ws is
 // the edge value at step 0, q = 1/a.
@@ -479,14 +489,16 @@ __device__ __noinline__ Span row_span(const RPrim& R, const PBox& bx, int32_t y,
         ta = -1;
         tb = T;
         wa0 = wa1 = wa2 = 0;
+        const bool s0 = stays_out(R.a0, ra), s1 = stays_out(R.a1, ra), s2 = stays_out(R.a2, ra);
         for (int64_t t = 0; t <= T; t++) {
             visited++;
-            const bool out = neg_product(w0, ra, rs) || neg_product(w1, ra, rs) || neg_product(w2, ra, rs);
-            if (out) {
+            const bool o0 = neg_product(w0, ra, rs), o1 = neg_product(w1, ra, rs), o2 = neg_product(w2, ra, rs);
+            if (o0 || o1 || o2) {
                 if (ta >= 0) {
                     tb = t - 1;
                     break;
                 }
+                if ((o0 && s0) || (o1 && s1) || (o2 && s2)) break;  // nothing covered from here on
             } else if (ta < 0) {
                 ta = t;
                 wa0 = w0;
@@ -579,6 +591,7 @@ __device__ __forceinline__ uint32_t walk_row(const RPrim& R, const PBox& bx, int
     const bool bias_zero = dbits(bias) == 0;
     const double ra = R.ra;
     const RaSign rs = ra_sign(ra);
+    const bool s0 = stays_out(R.a0, ra), s1 = stays_out(R.a1, ra), s2 = stays_out(R.a2, ra);
     uint32_t total = 0;
     bool was = false;
     for (int32_t x = bx.x0 + (int32_t)di; x <= bx.x1; x++) {
@@ -587,8 +600,11 @@ __device__ __forceinline__ uint32_t walk_row(const RPrim& R, const PBox& bx, int
         w1 = __dadd_rn(c1, R.a1);
         w2 = __dadd_rn(c2, R.a2);
         visited++;
-        if (neg_product(c0, ra, rs) || neg_product(c1, ra, rs) || neg_product(c2, ra, rs)) {
-            if (was) break;
+        const bool o0 = neg_product(c0, ra, rs), o1 = neg_product(c1, ra, rs), o2 = neg_product(c2, ra, rs);
+        if (o0 || o1 || o2) {
+            // rasterize breaks after the covered run; before it, an edge the
+            // row can only leave ends the row as well (nothing is covered later)
+            if (was || (o0 && s0) || (o1 && s1) || (o2 && s2)) break;
             continue;
         }
         was = true;
