@@ -140,6 +140,33 @@ __device__ void make_line_prims(const GeomParams& P, double line_width, uint64_t
     make_prim(P, slot + 1, s10, s11, s00, r1, r1, r0, v1, v1, v0, elem);
 }
 
+// clipPlanes (clipping.go:3-10): {P, N} of +x, -x, +y, -y, +z, -z.
+__device__ __forceinline__ void clip_plane(int k, D4& p, D4& n) {
+    double s = (k & 1) ? -1.0 : 1.0;
+    int axis = k >> 1;
+    p = d4(axis == 0 ? s : 0.0, axis == 1 ? s : 0.0, axis == 2 ? s : 0.0, 1.0);
+    n = d4(axis == 0 ? -s : 0.0, axis == 1 ? -s : 0.0, axis == 2 ? -s : 0.0, 1.0);
+}
+
+__device__ __forceinline__ bool point_in_front(int k, D4 v) {  // clipping.go:16-18
+    D4 p, n;
+    clip_plane(k, p, n);
+    return dot4(sub4(v, p), n) > 0;
+}
+
+// Whether sutherlandHodgman (clipping.go:28-52) leaves anything of a
+// triangle: planes the three vertices are all in front of pass the polygon
+// through unchanged, so at the first plane they are not all in front of,
+// no vertex in front means an empty result and some means real clipping.
+__device__ __forceinline__ bool clip_leaves_something(D4 a, D4 b, D4 c) {
+    for (int k = 0; k < 6; k++) {
+        const int in = (int)point_in_front(k, a) + (int)point_in_front(k, b) + (int)point_in_front(k, c);
+        if (in == 3) continue;
+        return in > 0;
+    }
+    return true;  // in front of every plane: ClipTriangle returns the triangle itself
+}
+
 // drawClippedTriangle's cull decision (context.go:322-336) on NDC x/y.
 // Returns +1 to draw in order (v0,v1,v2), -1 to draw swapped (v2,v1,v0),
 // 0 when culled.
@@ -222,7 +249,13 @@ __global__ void __launch_bounds__(kSetupTile) setup_kernel(GeomParams P) {
             u1 = I.mesh.corner_uniq[3 * t + 1];
             u2 = I.mesh.corner_uniq[3 * t + 2];
             clip = (vout[u0] | vout[u1] | vout[u2]) != 0;
-            if (!clip) {
+            if (clip) {
+                // a triangle the clipper empties needs no clip entry or slots
+                const VClip* vc = P.vclip + I.vbase;
+                const VClip a = vc[u0], b = vc[u1], c = vc[u2];
+                if (!clip_leaves_something(d4(a.x, a.y, a.z, a.w), d4(b.x, b.y, b.z, b.w), d4(c.x, c.y, c.z, c.w)))
+                    clip = false;  // order stays 0: no primitives
+            } else {
                 const double2* vndc = P.vndc + I.vbase;
                 double2 n0 = vndc[u0], n1 = vndc[u1], n2 = vndc[u2];
                 order = cull_decision(I.st, n0.x, n0.y, n1.x, n1.y, n2.x, n2.y);
@@ -257,20 +290,6 @@ __global__ void __launch_bounds__(kSetupTile) setup_kernel(GeomParams P) {
 // ---------------------------------------------------------------------------
 // Clipping (clipping.go)
 // ---------------------------------------------------------------------------
-
-// clipPlanes (clipping.go:3-10): {P, N} of +x, -x, +y, -y, +z, -z.
-__device__ __forceinline__ void clip_plane(int k, D4& p, D4& n) {
-    double s = (k & 1) ? -1.0 : 1.0;
-    int axis = k >> 1;
-    p = d4(axis == 0 ? s : 0.0, axis == 1 ? s : 0.0, axis == 2 ? s : 0.0, 1.0);
-    n = d4(axis == 0 ? -s : 0.0, axis == 1 ? -s : 0.0, axis == 2 ? -s : 0.0, 1.0);
-}
-
-__device__ __forceinline__ bool point_in_front(int k, D4 v) {  // clipping.go:16-18
-    D4 p, n;
-    clip_plane(k, p, n);
-    return dot4(sub4(v, p), n) > 0;
-}
 
 __device__ __forceinline__ D4 intersect_segment(int k, D4 v0, D4 v1) {  // clipping.go:20-26
     D4 p, n;
