@@ -202,32 +202,47 @@ __device__ void emit_triangle(const GeomParams& P, const StateView& st, uint64_t
 // Triangles take one slot (six in wireframe), or 7x that when they need
 // clipping; lines always take two slots (dead when clipped away).
 // ---------------------------------------------------------------------------
-__device__ void setup_triangle(const GeomParams& P, const ItemView& I, uint32_t item, uint64_t k, uint64_t slot,
-                               uint64_t count, bool clip, int order, uint32_t u0, uint32_t u1, uint32_t u2) {
-    const uint64_t t = I.tri_first + k;
-    if (clip) {
-        uint32_t idx = atomicAdd(P.clip_count, 1u);
-        if (idx < P.clip_cap) {
-            P.clip_list[idx] = ClipEntry{slot, (uint32_t)t, item};
-        } else {
-            atomicOr(P.status, ST_CLIP_OVERFLOW);
-        }
-        return;
+__device__ __forceinline__ void append_clip(const GeomParams& P, uint32_t item, uint64_t t, uint64_t slot) {
+    uint32_t idx = atomicAdd(P.clip_count, 1u);
+    if (idx < P.clip_cap) {
+        P.clip_list[idx] = ClipEntry{slot, (uint32_t)t, item};
+    } else {
+        atomicOr(P.status, ST_CLIP_OVERFLOW);
     }
+}
+
+// One piece of a triangle that survived culling: the whole triangle, or in
+// wireframe its edge `piece` (two primitives at slot + 2*piece).
+__device__ void emit_triangle_piece(const GeomParams& P, const ItemView& I, uint64_t t, uint64_t slot, int order,
+                                    uint32_t u0, uint32_t u1, uint32_t u2, uint32_t piece) {
     uint32_t c0 = (uint32_t)(3 * t), c1 = c0 + 1, c2 = c0 + 2;
     if (order < 0) {  // swap v0 <-> v2
         uint32_t tu = u0; u0 = u2; u2 = tu;
         uint32_t tc = c0; c0 = c2; c2 = tc;
     }
     const VScreen* vscr = P.vscr + I.vbase;
-    VScreen a = vscr[u0], b = vscr[u1], c = vscr[u2];
-    emit_triangle(P, I.st, slot, d3(a.x, a.y, a.z), d3(b.x, b.y, b.z), d3(c.x, c.y, c.z), a.rw, b.rw, c.rw, c0, c1,
-                  c2, (uint32_t)t);
+    if (!I.st.wireframe) {
+        const VScreen a = vscr[u0], b = vscr[u1], c = vscr[u2];
+        make_prim(P, slot, d3(a.x, a.y, a.z), d3(b.x, b.y, b.z), d3(c.x, c.y, c.z), a.rw, b.rw, c.rw, c0, c1, c2,
+                  (uint32_t)t);
+        return;
+    }
+    // wireframe: line(v0, v1), line(v1, v2), line(v2, v0) (context.go:296-301)
+    const uint32_t ua = piece == 0 ? u0 : piece == 1 ? u1 : u2;
+    const uint32_t ub = piece == 0 ? u1 : piece == 1 ? u2 : u0;
+    const uint32_t ca = piece == 0 ? c0 : piece == 1 ? c1 : c2;
+    const uint32_t cb = piece == 0 ? c1 : piece == 1 ? c2 : c0;
+    const VScreen a = vscr[ua], b = vscr[ub];
+    make_line_prims(P, I.st.line_width, slot + 2 * piece, d3(a.x, a.y, a.z), d3(b.x, b.y, b.z), a.rw, b.rw, ca, cb,
+                    (uint32_t)t);
 }
 
 __global__ void __launch_bounds__(kSetupTile) setup_kernel(GeomParams P) {
     __shared__ uint32_t s_tile;
     __shared__ OrderedAllocSmem<kSetupTile> s_alloc;
+    __shared__ uint64_t s_slot[kSetupTile];
+    __shared__ uint4 s_elem[kSetupTile];            // u0, u1, u2, cull order
+    __shared__ uint16_t s_work[3 * kSetupTile];     // element | piece << 8
     const uint32_t tile = block_ticket<kSetupTile>(P.lb, &s_tile);
     const uint32_t item = find_item(P.starts.stile, P.nitems, tile);
     const ItemView& I = P.items[item];
@@ -267,24 +282,52 @@ __global__ void __launch_bounds__(kSetupTile) setup_kernel(GeomParams P) {
     }
     const uint64_t slot = ordered_alloc<kSetupTile>(P.lb, tile, count, s_alloc);
     if (lt == 0 && threadIdx.x == 0) P.iout[item].prim_start = slot;  // thread 0's local prefix is 0
-    if (!valid || count == 0) return;
-    if (tri) {
-        setup_triangle(P, I, item, k, slot, count, clip, order, u0, u1, u2);
-        return;
+
+    // Clip entries are appended here; the primitive-emitting work (a
+    // triangle, each edge of a wireframe triangle, or a line) is packed onto
+    // consecutive threads so that culled elements leave no idle lanes in the
+    // FP64 setup arithmetic.
+    uint32_t work = 0;
+    if (valid && count != 0) {
+        if (tri) {
+            if (clip) append_clip(P, item, I.tri_first + k, slot);
+            else work = I.st.wireframe ? 3 : 1;
+        } else {
+            const uint64_t cb = 3 * I.mesh.ntri + 2 * (I.line_first + k);
+            u0 = I.mesh.corner_uniq[cb];
+            u1 = I.mesh.corner_uniq[cb + 1];
+            if ((vout[u0] | vout[u1]) != 0) {
+                uint32_t idx = atomicAdd(P.lclip_count, 1u);
+                P.lclip_list[idx] = ClipEntry{slot, (uint32_t)(I.line_first + k), item};  // holds every line of the pass
+            } else {
+                work = 1;
+            }
+        }
     }
-    const uint64_t l = I.line_first + k;
-    const uint64_t cb = 3 * I.mesh.ntri + 2 * l;
-    u0 = I.mesh.corner_uniq[cb];
-    u1 = I.mesh.corner_uniq[cb + 1];
-    if ((vout[u0] | vout[u1]) != 0) {
-        uint32_t idx = atomicAdd(P.lclip_count, 1u);
-        P.lclip_list[idx] = ClipEntry{slot, (uint32_t)l, item};  // lclip_list holds every line of the pass
-        return;
+    uint64_t wagg;
+    const uint32_t wpos = (uint32_t)block_exclusive_scan<kSetupTile>(work, s_alloc.warp, &wagg);
+    if (work) {
+        s_slot[threadIdx.x] = slot;
+        s_elem[threadIdx.x] = make_uint4(u0, u1, u2, (uint32_t)order);
+        for (uint32_t w = 0; w < work; w++) s_work[wpos + w] = (uint16_t)(threadIdx.x | (w << 8));
     }
-    const VScreen* vscr = P.vscr + I.vbase;
-    VScreen a = vscr[u0], b = vscr[u1];
-    make_line_prims(P, I.st.line_width, slot, d3(a.x, a.y, a.z), d3(b.x, b.y, b.z), a.rw, b.rw, (uint32_t)cb,
-                    (uint32_t)(cb + 1), kLineFlag | (uint32_t)l);
+    __syncthreads();
+    const uint32_t nwork = (uint32_t)wagg;
+    const uint64_t k0 = (uint64_t)(tri ? lt : lt - I.ntri_tiles) * kSetupTile;
+    for (uint32_t i = threadIdx.x; i < nwork; i += kSetupTile) {
+        const uint32_t j = s_work[i] & 0xFFu, piece = s_work[i] >> 8;
+        const uint4 e = s_elem[j];
+        if (tri) {
+            emit_triangle_piece(P, I, I.tri_first + k0 + j, s_slot[j], (int)e.w, e.x, e.y, e.z, piece);
+        } else {
+            const uint64_t l = I.line_first + k0 + j;
+            const uint64_t cb = 3 * I.mesh.ntri + 2 * l;
+            const VScreen* vscr = P.vscr + I.vbase;
+            const VScreen a = vscr[e.x], b = vscr[e.y];
+            make_line_prims(P, I.st.line_width, s_slot[j], d3(a.x, a.y, a.z), d3(b.x, b.y, b.z), a.rw, b.rw,
+                            (uint32_t)cb, (uint32_t)(cb + 1), kLineFlag | (uint32_t)l);
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
