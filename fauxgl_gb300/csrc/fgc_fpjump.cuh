@@ -58,6 +58,15 @@ FGC_HD double fj_add(double x, double y) {
 #endif
 }
 
+// Whether x * y <= z, without overflow.
+FGC_HD bool fj_mul_fits(uint64_t x, uint64_t y, uint64_t z) {
+#ifdef __CUDA_ARCH__
+    return __umul64hi(x, y) == 0 && x * y <= z;
+#else
+    return (unsigned __int128)x * y <= z;
+#endif
+}
+
 // t = s; repeat k times: t = RN(t + a). Returns t.
 FGC_HD double repeat_add(double s, double a, uint64_t k) {
     const uint64_t kSign = 0x8000000000000000ull;
@@ -105,17 +114,19 @@ FGC_HD double repeat_add(double s, double a, uint64_t k) {
         if (d == 0) return s;               // t + a rounds back to t from here on
         // steps that keep every exact sum (before rounding) inside the
         // binade, with one unit of margin at both ends
-        uint64_t n;
+        uint64_t avail;  // n steps fit when (n - 1) * d <= avail
         if (grow) {
             const uint64_t lim = kTop - 2;  // m_i + q <= 2^53 - 2
             if (m + q > lim) continue;
-            n = (lim - m - q) / d + 1;
+            avail = lim - m - q;
         } else {
             const uint64_t lim = kHidden + 1;  // m_i - q >= 2^52 + 1
             if (m < q + lim) continue;
-            n = (m - q - lim) / d + 1;
+            avail = m - q - lim;
         }
-        if (n > k) n = k;
+        // all k remaining steps usually fit: only a jump that reaches the
+        // binade's end needs the division
+        const uint64_t n = fj_mul_fits(k - 1, d, avail) ? k : avail / d + 1;
         m = grow ? m + n * d : m - n * d;
         k -= n;
         s = fj_double((sb & kSign) | ((uint64_t)es << 52) | (m - kHidden));
