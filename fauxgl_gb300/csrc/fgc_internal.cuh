@@ -161,6 +161,7 @@ struct RasterParams {
     int32_t F;                  // fragment buffer capacity
     int32_t Lmax;               // largest band of the pass (depth staging)
     int32_t win;                // fragment offsets a thread walks per round (wide primitives)
+    int32_t su;                 // units a chunk of wide primitives holds
     const PoolVertex* pool;
     const PoolVertex32* pool32;
     const float4* rf;
@@ -204,9 +205,15 @@ __global__ void fp64_rate_kernel(double* out, double a, double b, int iters);
 // Pixel buckets of the raster kernel's per-chunk fragment lists.
 constexpr int kRasterHeads = 2048;
 
-// (primitive, row) units a chunk of wide primitives holds; a band has at most
-// this many rows.
-constexpr int kSpanUnits = 128;
+// Rows of a band at most.
+constexpr int kBandRowsMax = 128;
+
+// (primitive, row) units a chunk of wide primitives holds: kSpanUnitsMax
+// where shared memory allows it without a smaller fragment buffer, else
+// kSpanUnitsMin. A primitive with more rows in a band than a chunk holds
+// (wrap-around rows of a box beyond the frame's sides) is split over chunks.
+constexpr int kSpanUnitsMin = 128;
+constexpr int kSpanUnitsMax = 256;
 
 // Bin entries a raster thread examines per chunk, and the chunk's primitive
 // capacity (a chunk of narrow primitives may hold several units per thread).
@@ -214,20 +221,20 @@ constexpr int kChunkPer = 1;
 constexpr int kChunkPrims = 256 * kChunkPer;
 
 // Dynamic shared memory of the raster kernel (layout in fgc_raster.cu), for
-// a fragment buffer of F: depth[L] f64, fragment b0/b1/b2/z[F] f64, span
-// edge values[kSpanUnits] 3 x f64, scratch 64 u64, fragment key/colour[F]
-// u32, unit slot/row[F] u32, span x/count/offset[kSpanUnits] u32, chunk
+// a fragment buffer of F and su span units: depth[L] f64, fragment
+// b0/b1/b2/z[F] f64, span edge values[su] 3 x f64, scratch 64 u64, fragment
+// key/colour[F] u32, unit slot/row[F] u32, span x/count/offset[su] u32, chunk
 // primitives[kChunkPrims] u32, bucket list heads[kRasterHeads] u16, list
 // links[F] u16, flags[F] u8. The colour buffer is not staged: the band's
 // pixels are read and written in global memory by the CTA that owns them.
-__host__ __device__ inline size_t raster_smem_bytes(int64_t L, int F, int threads) {
+__host__ __device__ inline size_t raster_smem_bytes(int64_t L, int F, int threads, int su) {
     size_t b = 0;
     b += (size_t)L * 8;
     b += (size_t)F * 8 * 4;
-    b += (size_t)kSpanUnits * 8 * 3;
+    b += (size_t)su * 8 * 3;
     b += 64 * 8;
     b += (size_t)F * 4 * 4;
-    b += (size_t)kSpanUnits * 4 * 3;
+    b += (size_t)su * 4 * 3;
     b += (size_t)(threads > kChunkPrims ? threads : kChunkPrims) * 4;
     b += (size_t)kRasterHeads * 2;
     b += (size_t)F * 2;

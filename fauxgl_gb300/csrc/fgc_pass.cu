@@ -64,6 +64,7 @@ struct PassPlan {
     int32_t Lmax = 1, band_rows = 1, Rmax = 1;
     int precision = FGC_PRECISION_PLAIN;
     int F = 0;
+    int su = kSpanUnitsMin;
     size_t smem = 0;
     int bin_warps = 1;
     uint32_t scan_tiles = 1;
@@ -93,23 +94,32 @@ std::vector<std::vector<uint32_t>> split_passes(const std::vector<PassItem>& ite
     return out;
 }
 
-int fit_fragments(const DevLimits& D, const PassTuning& T, int precision, int32_t Lmax, int& F, size_t& smem) {
+int fit_fragments(const DevLimits& D, const PassTuning& T, int precision, int32_t Lmax, int& F, int& su,
+                  size_t& smem) {
     const int stat = D.raster_static[precision == FGC_PRECISION_MIXED ? 1 : 0];
     const long two_cta = (long)D.smem_per_sm / 2 - D.smem_reserved_per_block - stat;
     const long one_cta = (long)D.smem_per_block_optin - stat;
     F = std::max(256, std::min(T.frag_cap, 4096));
-    smem = raster_smem_bytes(Lmax, F, kRasterThreads);
+    su = kSpanUnitsMin;
+    smem = raster_smem_bytes(Lmax, F, kRasterThreads, su);
     // two CTAs per SM (the register budget allows two) when a smaller
     // fragment buffer makes them fit
     while ((long)smem > two_cta && F > 512) {
         F -= 128;
-        smem = raster_smem_bytes(Lmax, F, kRasterThreads);
+        smem = raster_smem_bytes(Lmax, F, kRasterThreads, su);
     }
     while ((long)smem > one_cta && F > 256) {
         F /= 2;
-        smem = raster_smem_bytes(Lmax, F, kRasterThreads);
+        smem = raster_smem_bytes(Lmax, F, kRasterThreads, su);
     }
     if ((long)smem > one_cta) return fail(FGC_ERR_UNSUPPORTED, "frame too wide for the band rasteriser");
+    // the larger span chunk where it costs neither fragments nor a CTA per SM
+    const long budget = (long)smem <= two_cta ? two_cta : one_cta;
+    const size_t wide = raster_smem_bytes(Lmax, F, kRasterThreads, kSpanUnitsMax);
+    if ((long)wide <= budget) {
+        su = kSpanUnitsMax;
+        smem = wide;
+    }
     return FGC_OK;
 }
 
@@ -141,7 +151,7 @@ int plan_pass(const Submission& sub, const std::vector<uint32_t>& idx, const Dev
         v.H = c->H;
         v.N = c->N;
         int64_t R = std::max<int64_t>(1, T.band_pixels / c->W);
-        R = std::min<int64_t>(R, kSpanUnits);  // a band's rows of one primitive fit one chunk
+        R = std::min<int64_t>(R, kBandRowsMax);
         R = std::min<int64_t>(R, c->H);
         if (R * c->W > 65535) return fail(FGC_ERR_UNSUPPORTED, "frame width above 65535 pixels is not supported");
         v.R = (int32_t)R;
@@ -204,7 +214,7 @@ int plan_pass(const Submission& sub, const std::vector<uint32_t>& idx, const Dev
     P.band[n] = P.nbands;
     if (P.nmat >= 0xFFFFFFFFull) return fail(FGC_ERR_UNSUPPORTED, "pass too large for its bin matrix");
     P.scan_tiles = (uint32_t)ceil_div(P.nmat, 2048);
-    int rc = fit_fragments(D, T, P.precision, P.Lmax, P.F, P.smem);
+    int rc = fit_fragments(D, T, P.precision, P.Lmax, P.F, P.su, P.smem);
     if (rc) return rc;
     const int warps = (int)std::min<int64_t>(8, (96 * 1024) / ((int64_t)P.max_nbands * 4));
     if (warps < 1) return fail(FGC_ERR_UNSUPPORTED, "frame has too many bands for binning");
@@ -479,6 +489,7 @@ int issue_submission(PassScratch& S, cudaStream_t stream, const DevLimits& D, co
         rp.F = P.F;
         rp.Lmax = P.Lmax;
         rp.win = std::max(1, std::min(T.window, 256));
+        rp.su = P.su;
         rp.pool = S.pool.p;
         rp.pool32 = S.pool32.p;
         rp.rf = S.rf.p;

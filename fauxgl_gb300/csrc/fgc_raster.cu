@@ -47,14 +47,14 @@ struct RasterSmem {
     double* fz;
     uint32_t* fkey;  // [F] (pixel << 16) | unit
     uint32_t* fcol;  // [F] NRGBA
-    double* uw0;     // [kSpanUnits] unit -> edge values at its first covered in-band pixel
+    double* uw0;     // [su] unit -> edge values at its first covered in-band pixel
     double* uw1;
     double* uw2;
     uint32_t* uslot; // [F] unit -> chunk slot
     int32_t* urow;   // [F] unit -> row y
-    int32_t* ux;     // [kSpanUnits] unit -> first covered in-band x
-    uint32_t* ucnt;  // [kSpanUnits] unit -> covered in-band pixels
-    uint32_t* ufrag; // [kSpanUnits] unit -> first fragment offset in the chunk
+    int32_t* ux;     // [su] unit -> first covered in-band x
+    uint32_t* ucnt;  // [su] unit -> covered in-band pixels
+    uint32_t* ufrag; // [su] unit -> first fragment offset in the chunk
     uint32_t* cprim; // [kChunkPrims] chunk slot -> primitive
     unsigned short* head;  // [kHeads] per pixel bucket: last fragment of its list (0xFFFF: none)
     unsigned short* nxt;   // [F] per fragment: the previous fragment in its bucket
@@ -853,11 +853,13 @@ struct ChunkEntry {
 };
 
 __device__ __forceinline__ ChunkEntry chunk_entry(const RasterParams& P, const ItemView& I, const BandCtx& B,
-                                                  uint64_t at, bool box_bound) {
+                                                  uint64_t at, bool box_bound, uint32_t roff) {
     ChunkEntry c;
     c.p = P.bins[at];
     const PBox bx = P.pbox[c.p];
     rows_in_band(bx, I.W, B, c.ylo, c.nrows);
+    c.ylo += (int32_t)roff;  // rows an earlier chunk took
+    c.nrows -= (int32_t)roff;
     int64_t wid = (int64_t)bx.x1 - bx.x0 + 1;
     c.narrow = wid <= kNarrow;
     if (!box_bound && (int64_t)P.pspan[c.p] < wid) wid = P.pspan[c.p];
@@ -904,23 +906,23 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
         S.fb1 = (double*)q; q += (size_t)F * 8;
         S.fb2 = (double*)q; q += (size_t)F * 8;
         S.fz = (double*)q; q += (size_t)F * 8;
-        S.uw0 = (double*)q; q += (size_t)kSpanUnits * 8;
-        S.uw1 = (double*)q; q += (size_t)kSpanUnits * 8;
-        S.uw2 = (double*)q; q += (size_t)kSpanUnits * 8;
+        S.uw0 = (double*)q; q += (size_t)P.su * 8;
+        S.uw1 = (double*)q; q += (size_t)P.su * 8;
+        S.uw2 = (double*)q; q += (size_t)P.su * 8;
         S.scratch = (unsigned long long*)q; q += 64 * 8;
         S.fkey = (uint32_t*)q; q += (size_t)F * 4;
         S.fcol = (uint32_t*)q; q += (size_t)F * 4;
         S.uslot = (uint32_t*)q; q += (size_t)F * 4;
         S.urow = (int32_t*)q; q += (size_t)F * 4;
-        S.ux = (int32_t*)q; q += (size_t)kSpanUnits * 4;
-        S.ucnt = (uint32_t*)q; q += (size_t)kSpanUnits * 4;
-        S.ufrag = (uint32_t*)q; q += (size_t)kSpanUnits * 4;
+        S.ux = (int32_t*)q; q += (size_t)P.su * 4;
+        S.ucnt = (uint32_t*)q; q += (size_t)P.su * 4;
+        S.ufrag = (uint32_t*)q; q += (size_t)P.su * 4;
         S.cprim = (uint32_t*)q; q += kChunkPrims * 4;
         S.head = (unsigned short*)q; q += (size_t)kRasterHeads * 2;
         S.nxt = (unsigned short*)q; q += (size_t)F * 2;
         S.fflag = (uint8_t*)q;
     }
-    __shared__ uint32_t s_band, s_item, s_nfrag, s_conflict, s_nprim, s_nunit, s_ftotal, s_mode, s_bsum, s_ratio;
+    __shared__ uint32_t s_band, s_item, s_nfrag, s_conflict, s_nprim, s_nunit, s_ftotal, s_mode, s_bsum, s_ratio, s_split;
     __shared__ uint64_t s_warp[kRT / 32 + 1];
     __shared__ ItemView s_iv;  // the draw of the current band
     const ItemView& I = s_iv;
@@ -972,7 +974,8 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
         __syncthreads();
 
         uint64_t k = 0;
-        int level = 0;  // 0: estimated fragments, 1: widest-chord bound, 2: box bound
+        uint32_t roff = 0;  // rows of the entry at k taken by earlier chunks
+        int level = 0;      // 0: estimated fragments, 1: widest-chord bound, 2: box bound
         while (k < bcount) {
             // ---- chunk: a prefix of the remaining bin; thread t examines
             // entries k + kChunkPer*t + j. The first primitive picks how the
@@ -985,41 +988,55 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
             //           chunks (early depth rejection makes it small); a walk
             //           that outgrows F is redone at level 1 with the bound
             //           itself, then at level 2 with the box width
-            //   spans   anything else, at most kSpanUnits units: spans, then
+            //   spans   anything else, at most P.su units: spans, then
             //           windows of fragment offsets
+            // An entry with more rows in the band than its chunk holds (rows
+            // that wrap around the frame's sides) goes alone, its rows over
+            // several chunks.
             const uint64_t e0 = k + (uint64_t)threadIdx.x * kChunkPer;
             ChunkEntry ce[kChunkPer];
 #pragma unroll
             for (int j = 0; j < kChunkPer; j++)
-                ce[j] = (e0 + j < bcount) ? chunk_entry(P, I, B, bstart + e0 + j, level == 2) : ChunkEntry{0, 0, 0, 0, true};
+                ce[j] = (e0 + j < bcount)
+                            ? chunk_entry(P, I, B, bstart + e0 + j, level == 2, (e0 + j == k) ? roff : 0u)
+                            : ChunkEntry{0, 0, 0, 0, true};
             if (threadIdx.x == 0) {
-                s_mode = (ce[0].narrow && ce[0].bound <= (uint32_t)F) ? 1u : 0u;
+                const bool dm = ce[0].narrow && ce[0].bound <= (uint32_t)F;
+                // a direct chunk holds at most one unit per thread: a second
+                // pass over the units would double its first warps' walk
+                const uint32_t cap0 = dm ? (uint32_t)min(F, kRT) : (uint32_t)P.su;
+                s_mode = dm ? 1u : 0u;
+                s_split = ((uint32_t)ce[0].nrows > cap0) ? cap0 : 0u;
                 s_nprim = 0;
                 s_nunit = 0;
                 s_bsum = 0;
             }
             __syncthreads();
             const bool direct = s_mode != 0;
+            const uint32_t split = s_split;  // rows of the entry at k this chunk takes, when it goes alone
             const uint32_t ratio = level == 0 ? s_ratio : kRatioOne;
-            // a direct chunk holds at most one unit per thread: a second pass
-            // over the units would double its first warps' walk
-            const uint64_t ucap = direct ? (uint64_t)min(F, kRT) : (uint64_t)kSpanUnits;
+            const uint64_t ucap = direct ? (uint64_t)min(F, kRT) : (uint64_t)P.su;
+            const int jmax = split ? (threadIdx.x == 0 ? 1 : 0) : kChunkPer;
+            if (split && threadIdx.x == 0) ce[0].nrows = (int32_t)split;
             uint64_t tkey = 0, tun = 0;
 #pragma unroll
             for (int j = 0; j < kChunkPer; j++) {
+                if (j >= jmax) break;
                 tkey += chunk_key(ce[j], direct, ratio, F);
                 tun += (uint64_t)ce[j].nrows;
             }
             uint64_t kagg, uagg;
             uint64_t kr = block_exclusive_scan<kRT>(tkey, s_warp, &kagg);
             uint64_t ur = block_exclusive_scan<kRT>(tun, s_warp, &uagg);
-            // the entries inside the prefix (never empty: R <= kSpanUnits, and
-            // a direct chunk's first estimate is at most its bound <= F)
+            // the entries inside the prefix (never empty: the first entry's
+            // rows fit, and a direct chunk's first estimate is at most its
+            // bound <= F)
             {
                 const uint64_t ur0 = ur;
                 uint32_t took = 0, bsum = 0;
 #pragma unroll
                 for (int j = 0; j < kChunkPer; j++) {
+                    if (j >= jmax) break;
                     const uint64_t key = chunk_key(ce[j], direct, ratio, F);
                     if (e0 + j >= bcount || ur + (uint64_t)ce[j].nrows > ucap || kr + key > (uint64_t)F) break;
                     const uint32_t slot = threadIdx.x * kChunkPer + j;
@@ -1078,7 +1095,12 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
                 }
                 if (redo && threadIdx.x == 0) atomicOr(P.status, ST_RASTER_INTERNAL);
                 level = 0;
-                k += nprim;
+                if (split) {
+                    roff += split;
+                } else {
+                    k += nprim;
+                    roff = 0;
+                }
                 continue;
             }
             level = 0;
@@ -1097,7 +1119,7 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
             __syncthreads();
             // ---- fragment offsets of the units, in unit order
             {
-                const uint32_t per = ((uint32_t)kSpanUnits + kRT - 1) / kRT;
+                const uint32_t per = ((uint32_t)P.su + kRT - 1) / kRT;
                 const uint32_t u0 = threadIdx.x * per;
                 uint64_t local = 0;
                 for (uint32_t j = 0; j < per; j++)
@@ -1162,7 +1184,12 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
                 resolve_chunk(P, I, B, S, nfrag, (s_conflict & 1u) != 0, upd);
                 __syncthreads();
             }
-            k += nprim;
+            if (split) {
+                roff += split;
+            } else {
+                k += nprim;
+                roff = 0;
+            }
         }
         for (int j = threadIdx.x; j < npx; j += blockDim.x) I.depth[B.i0 + j] = S.depth[j];
         __syncthreads();

@@ -138,6 +138,21 @@ def test_row_wraparound(gpu_lib, alpha):
     p.check()
 
 
+@pytest.mark.parametrize("alpha", [1.0, 0.5])
+def test_wrapped_rows_beyond_a_chunk(gpu_lib, alpha):
+    """Line quads hundreds of pixels wider than a 2-pixel frame: in each band
+    their wrapped rows outnumber the units one chunk holds, so the
+    rasteriser takes such a primitive alone, its rows over several chunks."""
+    w, h = 2, 300
+    pts = [((0.5, 10.0), (1.5, 290.0)), ((1.0, 150.0), (1.2, 160.0)), ((0.1, 299.0), (1.9, 0.5))]
+    lp = np.array([[[*screen_to_ndc(x, y, w, h), 0.0] for (x, y) in seg] for seg in pts])
+    line = Mesh(None, line_pos=lp)
+    p = Pair(w, h)
+    p.clear_color((0, 0, 0, 1))
+    run_both(p, line, state(line_width=400.0), solid((1, 1, 1, alpha)), what=2)
+    p.check()
+
+
 # ---------------------------------------------------------------------------
 # seeded random scenes over the draw state space
 # ---------------------------------------------------------------------------
