@@ -68,6 +68,10 @@ def parse():
     ap.add_argument("--ss-steps", type=int, default=5, help="timed frames of the 16x supersampled variants")
     ap.add_argument("--cpu-frames", type=int, default=5)
     ap.add_argument("--batch-steps", type=int, default=5, help="timed batches of the 1,024-view thumbnail batch")
+    ap.add_argument("--batch-views", type=int, default=0,
+                    help="render only the first N views of the thumbnail batch (0: all; for profiler runs)")
+    ap.add_argument("--batch-tuning", default="auto",
+                    help="'auto' (autotune) or band_pixels,prims_per_bin_block,fragment_cap,window")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per rate of the serving loop")
     ap.add_argument("--serve-max-requests", type=int, default=160, help="requests per rate at most")
     ap.add_argument("--serve-budget-gb", type=int, default=96, help="HBM budget of the serving loop")
@@ -159,7 +163,8 @@ class ClockSampler:
 
 def work_dict(s):
     return {k: int(getattr(s, k)) for k in ("elements", "clipped", "primitives", "bin_entries", "visited_pixels",
-                                            "covered_pixels", "shaded_fragments", "updated_pixels")}
+                                            "covered_pixels", "shaded_fragments", "updated_pixels", "attempts",
+                                            "kernel_launches")}
 
 
 class Frame:
@@ -270,6 +275,8 @@ def bench_batch(lib, args, torch):
     from fauxgl_gb300.shader import NewPhongShader, to_fgc_shader
     t0 = time.time()
     meshes, views = scenes.thumbnail_batch()
+    if args.batch_views > 0:
+        views = views[:args.batch_views]
     handles = [_upload_mesh(m) for m in meshes]
     log("batch scene: %d meshes, %d views, %d triangles drawn per batch (%.1fs)" % (
         len(meshes), len(views), sum(meshes[v["mesh"]].ntri for v in views), time.time() - t0))
@@ -328,8 +335,13 @@ def bench_batch(lib, args, torch):
 
     # autotune the pipeline shapes on this batch (results never depend on them)
     tuned = _abi.FgcBatchTuning()
-    clears()
-    _abi.check(lib.fgc_batch_autotune(b, items, n, 1, ctypes.byref(tuned)))
+    if args.batch_tuning == "auto":
+        clears()
+        _abi.check(lib.fgc_batch_autotune(b, items, n, 1, ctypes.byref(tuned)))
+    else:
+        bp, pb, fc, win = (int(x) for x in args.batch_tuning.split(","))
+        tuned = _abi.FgcBatchTuning(bp, pb, fc, 0, win, 0)
+        _abi.check(lib.fgc_batch_set_tuning(b, ctypes.byref(tuned)))
     tuning = {k: int(getattr(tuned, k)) for k, _ in _abi.FgcBatchTuning._fields_}
     log("batch tuning:", tuning)
     steps = max(3, args.batch_steps)
@@ -596,7 +608,8 @@ def main():
     if args.only == "ss16":
         f = Frame(lib, mesh_h, W * SS, H * SS, _abi.FGC_PRECISION_PLAIN, overlay=True, scale=SS)
         ss_ms, _ = time_frames(f, args.steps, args.warmup, torch, barrier)
-        print(json.dumps({"ss16_plain_ms_per_frame": round(ss_ms, 3), "steps": args.steps}), flush=True)
+        print(json.dumps({"ss16_plain_ms_per_frame": round(ss_ms, 3), "steps": args.steps,
+                          "work": {"surface": f.pass_work[0], "overlay": f.pass_work[1]}}), flush=True)
         f.close()
         return 0
     if args.only == "batch":
