@@ -26,4 +26,7 @@ def __getattr__(name):
                 "CullBack", "PRECISION_PLAIN", "PRECISION_MIXED"):
         from . import context
         return getattr(context, name)
+    if name in ("LoadSTL", "DeviceMesh"):
+        from . import meshops
+        return getattr(meshops, name)
     raise AttributeError(name)

@@ -147,6 +147,12 @@ SIGNATURES = {
     "fgc_mesh_upload": (_I, [_D, _D, _D, _D, _U64, _D, _D, _D, _D, _U64, _PP]),
     "fgc_mesh_release": (_I, [_P]),
     "fgc_mesh_counts": (_I, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
+    "fgc_mesh_load_stl": (_I, [ctypes.c_void_p, _U64, _PP]),
+    "fgc_mesh_smooth_normals_threshold": (_I, [_P, ctypes.c_double]),
+    "fgc_mesh_smooth_normals": (_I, [_P]),
+    "fgc_mesh_sharp_edges": (_I, [_P, ctypes.c_double, _PP]),
+    "fgc_mesh_silhouette": (_I, [_P, _D, ctypes.c_double, _PP]),
+    "fgc_mesh_download": (_I, [_P, _D, _D, _D, _D]),
     "fgc_texture_upload": (_I, [ctypes.POINTER(ctypes.c_uint16), _I32, _I32, _PP]),
     "fgc_texture_release": (_I, [_P]),
     "fgc_draw_mesh": (_I, [_P, _P, _ST, _SH, _INFO]),

@@ -19,7 +19,7 @@ LIB = os.path.join(HERE, "libfauxglcuda.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr"]
-SOURCES = ["fgc_api.cu", "fgc_pass.cu", "fgc_batch.cu", "fgc_geometry.cu", "fgc_bin.cu", "fgc_raster.cu",
+SOURCES = ["fgc_api.cu", "fgc_pass.cu", "fgc_batch.cu", "fgc_geometry.cu", "fgc_bin.cu", "fgc_raster.cu", "fgc_meshops.cu",
            "fgc_misc.cu"]
 
 

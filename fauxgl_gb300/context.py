@@ -44,8 +44,12 @@ class RasterizeInfo(namedtuple("RasterizeInfo", "TotalPixels UpdatedPixels")):
 
 
 def _upload_mesh(mesh):
-    """Device handle of a Mesh, uploaded once and cached on the mesh."""
+    """Device handle of a Mesh, uploaded once and cached on the mesh (a
+    meshops.DeviceMesh is already on the device)."""
     lib = _abi.load_library()
+    from .meshops import DeviceMesh
+    if isinstance(mesh, DeviceMesh):
+        return mesh.handle
     if mesh._device is not None:
         return mesh._device.handle
     keep = []

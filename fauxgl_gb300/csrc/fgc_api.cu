@@ -186,6 +186,68 @@ int draw(fgc_context* c, const fgc_mesh* m, uint64_t tf, uint64_t tc, uint64_t l
 // ===========================================================================
 // C ABI
 // ===========================================================================
+// Weld the corner positions cp (device, 3 per corner) and fill the mesh's
+// unique-position arrays, corner index and position/normal records (nrm may
+// be null: zero normals). Runs on stream s and waits for it.
+int mesh_weld_attrs(fgc_mesh* m, cudaStream_t s, int sms, const double* cp, const double* nrm, uint64_t V) {
+    int rc = FGC_OK;
+    DevBuf<uint32_t> table, slot_of, minc, flag, uid;
+    DevBuf<unsigned long long> tiles;
+    DevBuf<unsigned int> st, tick;
+    unsigned long long* h_tot = nullptr;
+    auto step = [&](cudaError_t err, const char* what) {
+        if (err != cudaSuccess && rc == FGC_OK) rc = fail(FGC_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(err));
+        return rc == FGC_OK;
+    };
+    const int grid = grid_for(V, 256, sms * 16);
+    do {
+        // weld positions
+        uint64_t tsize = 1;
+        while (tsize < 2 * V) tsize <<= 1;
+        if (!step(table.ensure(tsize), "alloc weld table")) break;
+        if (!step(minc.ensure(tsize), "alloc weld table")) break;
+        if (!step(slot_of.ensure(V), "alloc weld") || !step(flag.ensure(V), "alloc weld") || !step(uid.ensure(V), "alloc weld")) break;
+        if (!step(st.ensure(1), "alloc status") || !step(cudaMemsetAsync(st.p, 0, 4, s), "zero status")) break;
+        if (!step(cudaMemsetAsync(table.p, 0xFF, tsize * 4, s), "init table")) break;
+        if (!step(cudaMemsetAsync(minc.p, 0xFF, tsize * 4, s), "init table")) break;
+        weld_insert_kernel<<<grid, 256, 0, s>>>(cp, V, table.p, tsize - 1, slot_of.p, minc.p, st.p);
+        weld_flag_kernel<<<grid, 256, 0, s>>>(slot_of.p, minc.p, V, flag.p);
+        const uint64_t scan_tiles = (V + 2047) / 2048;
+        if (!step(tiles.ensure(scan_tiles + 2), "alloc scan") || !step(cudaMemsetAsync(tiles.p, 0, (scan_tiles + 2) * 8, s), "zero scan")) break;
+        ScanParams sp;
+        sp.in = flag.p;
+        sp.out = uid.p;
+        sp.n = V;
+        sp.lb = Lookback{tiles.p + 1, (unsigned int*)(st.p), st.p, tiles.p};
+        // the scan's ticket counter and status share the zeroed status word's
+        // neighbour: use a dedicated zeroed word instead
+        if (!step(tick.ensure(1), "alloc ticket") || !step(cudaMemsetAsync(tick.p, 0, 4, s), "zero ticket")) break;
+        sp.lb.ticket = tick.p;
+        scan_u32_kernel<<<(unsigned)scan_tiles, 256, 0, s>>>(sp);
+        if (!step(cudaGetLastError(), "weld kernels")) break;
+        if (!step(cudaMallocHost((void**)&h_tot, 16), "alloc pinned")) break;
+        if (!step(cudaMemcpyAsync(h_tot, tiles.p, 8, cudaMemcpyDeviceToHost, s), "read unique count")) break;
+        if (!step(cudaMemcpyAsync(h_tot + 1, st.p, 4, cudaMemcpyDeviceToHost, s), "read status")) break;
+        if (!step(cudaStreamSynchronize(s), "weld")) break;
+        if (((unsigned int*)(h_tot + 1))[0] != 0) {
+            rc = fail(FGC_ERR_DEVICE_LIMIT, "mesh weld failed");
+            break;
+        }
+        m->nuniq = h_tot[0];
+        if (!step(m->ux.ensure(m->nuniq + 1), "alloc unique") || !step(m->uy.ensure(m->nuniq + 1), "alloc unique") ||
+            !step(m->uz.ensure(m->nuniq + 1), "alloc unique") || !step(m->corner_uniq.ensure(V), "alloc index"))
+            break;
+        weld_emit_kernel<<<grid, 256, 0, s>>>(cp, slot_of.p, minc.p, uid.p, V, m->ux.p, m->uy.p, m->uz.p,
+                                              m->corner_uniq.p);
+        if (!step(m->pn64.ensure(V), "alloc attributes") || !step(m->pn32.ensure(V), "alloc attributes")) break;
+        attrs_kernel<<<grid, 256, 0, s>>>(cp, nrm, V, m->pn64.p, m->pn32.p);
+        if (!step(cudaGetLastError(), "attribute kernels")) break;
+    } while (0);
+    cudaStreamSynchronize(s);
+    if (h_tot) cudaFreeHost(h_tot);
+    return rc;
+}
+
 extern "C" {
 
 int32_t fgc_abi_version(void) { return FGC_ABI_VERSION; }
@@ -405,11 +467,7 @@ int fgc_mesh_upload(const double* tri_pos, const double* tri_nrm, const double* 
         return fail(FGC_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
     }
     int rc = FGC_OK;
-    DevBuf<double> cp, nrm, tmp;
-    DevBuf<uint32_t> table, slot_of, minc, flag, uid;
-    DevBuf<unsigned long long> tiles;
-    DevBuf<unsigned int> st;
-    unsigned long long* h_tot = nullptr;
+    DevBuf<double> cp, nrm;
     auto step = [&](cudaError_t err, const char* what) {
         if (err != cudaSuccess && rc == FGC_OK) rc = fail(FGC_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(err));
         return rc == FGC_OK;
@@ -427,48 +485,8 @@ int fgc_mesh_upload(const double* tri_pos, const double* tri_nrm, const double* 
             if (tri_nrm && !step(cudaMemcpyAsync(nrm.p, tri_nrm, ntri * 9 * 8, cudaMemcpyHostToDevice, s), "copy normals")) break;
             if (line_nrm && !step(cudaMemcpyAsync(nrm.p + ntri * 9, line_nrm, nline * 6 * 8, cudaMemcpyHostToDevice, s), "copy normals")) break;
         }
-        // weld positions
-        uint64_t tsize = 1;
-        while (tsize < 2 * V) tsize <<= 1;
-        if (!step(table.ensure(tsize), "alloc weld table")) break;
-        if (!step(minc.ensure(tsize), "alloc weld table")) break;
-        if (!step(slot_of.ensure(V), "alloc weld") || !step(flag.ensure(V), "alloc weld") || !step(uid.ensure(V), "alloc weld")) break;
-        if (!step(st.ensure(1), "alloc status") || !step(cudaMemsetAsync(st.p, 0, 4, s), "zero status")) break;
-        if (!step(cudaMemsetAsync(table.p, 0xFF, tsize * 4, s), "init table")) break;
-        if (!step(cudaMemsetAsync(minc.p, 0xFF, tsize * 4, s), "init table")) break;
-        weld_insert_kernel<<<grid, 256, 0, s>>>(cp.p, V, table.p, tsize - 1, slot_of.p, minc.p, st.p);
-        weld_flag_kernel<<<grid, 256, 0, s>>>(slot_of.p, minc.p, V, flag.p);
-        const uint64_t scan_tiles = (V + 2047) / 2048;
-        if (!step(tiles.ensure(scan_tiles + 2), "alloc scan") || !step(cudaMemsetAsync(tiles.p, 0, (scan_tiles + 2) * 8, s), "zero scan")) break;
-        ScanParams sp;
-        sp.in = flag.p;
-        sp.out = uid.p;
-        sp.n = V;
-        sp.lb = Lookback{tiles.p + 1, (unsigned int*)(st.p), st.p, tiles.p};
-        // the scan's ticket counter and status share the zeroed status word's
-        // neighbour: use a dedicated zeroed word instead
-        DevBuf<unsigned int> tick;
-        if (!step(tick.ensure(1), "alloc ticket") || !step(cudaMemsetAsync(tick.p, 0, 4, s), "zero ticket")) break;
-        sp.lb.ticket = tick.p;
-        scan_u32_kernel<<<(unsigned)scan_tiles, 256, 0, s>>>(sp);
-        if (!step(cudaGetLastError(), "weld kernels")) break;
-        if (!step(cudaMallocHost((void**)&h_tot, 16), "alloc pinned")) break;
-        if (!step(cudaMemcpyAsync(h_tot, tiles.p, 8, cudaMemcpyDeviceToHost, s), "read unique count")) break;
-        if (!step(cudaMemcpyAsync(h_tot + 1, st.p, 4, cudaMemcpyDeviceToHost, s), "read status")) break;
-        if (!step(cudaStreamSynchronize(s), "weld")) break;
-        if (((unsigned int*)(h_tot + 1))[0] != 0) {
-            rc = fail(FGC_ERR_DEVICE_LIMIT, "mesh weld failed");
-            break;
-        }
-        m->nuniq = h_tot[0];
-        if (!step(m->ux.ensure(m->nuniq + 1), "alloc unique") || !step(m->uy.ensure(m->nuniq + 1), "alloc unique") ||
-            !step(m->uz.ensure(m->nuniq + 1), "alloc unique") || !step(m->corner_uniq.ensure(V), "alloc index"))
-            break;
-        weld_emit_kernel<<<grid, 256, 0, s>>>(cp.p, slot_of.p, minc.p, uid.p, V, m->ux.p, m->uy.p, m->uz.p,
-                                              m->corner_uniq.p);
-        if (!step(m->pn64.ensure(V), "alloc attributes") || !step(m->pn32.ensure(V), "alloc attributes")) break;
-        attrs_kernel<<<grid, 256, 0, s>>>(cp.p, have_nrm ? nrm.p : nullptr, V, m->pn64.p, m->pn32.p);
-        if (!step(cudaGetLastError(), "attribute kernels")) break;
+        rc = mesh_weld_attrs(m, s, sms, cp.p, have_nrm ? nrm.p : nullptr, V);
+        if (rc != FGC_OK) break;
         if (tri_tex || line_tex) {
             m->has_tex = true;
             if (!step(m->tex64.ensure(V * 2), "alloc texcoords") || !step(m->tex32.ensure(V * 2), "alloc texcoords")) break;
@@ -489,7 +507,6 @@ int fgc_mesh_upload(const double* tri_pos, const double* tri_nrm, const double* 
         step(cudaStreamSynchronize(s), "mesh upload");
     } while (0);
     cudaStreamSynchronize(s);
-    if (h_tot) cudaFreeHost(h_tot);
     cudaStreamDestroy(s);
     if (rc != FGC_OK) {
         delete m;

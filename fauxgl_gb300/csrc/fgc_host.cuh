@@ -142,6 +142,10 @@ struct fgc_mesh {
     }
 };
 
+// Weld device corner positions cp (3 doubles per corner) into m and fill its
+// position/normal records from nrm (device, or null for zero normals).
+int mesh_weld_attrs(fgc_mesh* m, cudaStream_t s, int sms, const double* cp, const double* nrm, uint64_t V);
+
 namespace fgc {
 
 // Pass-wide device counters (one block per pass; the status word is shared by

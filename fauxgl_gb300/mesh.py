@@ -4,11 +4,12 @@ The reference keeps a mesh as []*Triangle of 17-float64 Vertex values
 (mesh.go:9-13, triangle.go:3-5, vertex.go:3-12). Here a mesh is a set of
 per-corner float64 arrays (the triangle soup, no index sharing), which is what
 the device takes: tri_pos (T,3,3), tri_nrm (T,3,3), tri_tex (T,3,2),
-tri_col (T,3,4) and the same per line with 2 corners. The host-side mesh
-processing the examples run before drawing (BiUnitCube/FitInside, Transform,
-SmoothNormals[Threshold]) is restated with the reference's operation order so
-the arrays hold the bits the reference would hold. Citations are
-fogleman/fauxgl file:line.
+tri_col (T,3,4) and the same per line with 2 corners. BiUnitCube/FitInside and
+Transform are restated on the host with the reference's operation order;
+SmoothNormals[Threshold], SharpEdges and Silhouette run on the GPU
+(meshops.DeviceMesh). smooth_normals_threshold_host / smooth_normals_host are
+host restatements of the smoothing used to synthesise benchmark meshes where
+the library is not loaded. Citations are fogleman/fauxgl file:line.
 """
 import math
 
@@ -287,57 +288,96 @@ class Mesh:
         """mesh.go:122-125."""
         return self.FitInside((-0.5, -0.5, -0.5), (0.5, 0.5, 0.5), (0.5, 0.5, 0.5))
 
-    def _position_groups(self):
-        """Group corners by Position as Go's map[Vector] does (== on float64,
-        so -0 and +0 are one key). Returns (order, starts, counts) where
-        order lists corner indices grouped by key, each group in corner
-        (triangle, then V1..V3) order."""
-        p = self.tri_pos.reshape(-1, 3) + 0.0  # -0 -> +0
-        inv = group_rows(p)
-        order = np.argsort(inv, kind="stable")
-        counts = np.bincount(inv)
-        starts = np.concatenate([[0], np.cumsum(counts)[:-1]])
-        return inv, order, starts, counts
-
+    # -- on the GPU (meshops.DeviceMesh): upload, operate, read back ------------
     def SmoothNormalsThreshold(self, radians):
-        """mesh.go:80-103: each corner's normal becomes the normalised sum, in
-        corner order, of the normals at the same position whose dot product
-        with it is at least cos(radians)."""
-        threshold = math.cos(radians)
-        nrm = (self.tri_nrm if self.tri_nrm is not None else np.zeros_like(self.tri_pos)).reshape(-1, 3)
-        inv, order, starts, counts = self._position_groups()
-        gmax = int(counts.max()) if counts.size else 0
-        member = np.full((counts.size, gmax), -1, dtype=np.int64)
-        rank = np.arange(order.size) - np.repeat(starts, counts)
-        member[inv[order], rank] = order
-        acc = np.zeros_like(nrm)
-        mine = nrm
-        for k in range(gmax):
-            idx = member[inv, k]
-            valid = idx >= 0
-            x = nrm[np.where(valid, idx, 0)]
-            take = valid & (_dot(x, mine) >= threshold)
-            # adding +0 for a skipped normal leaves the running sum unchanged:
-            # the sum starts at +0 and is never -0
-            acc = acc + np.where(take[:, None], x, 0.0)
-        self.tri_nrm = _normalize(acc).reshape(-1, 3, 3)
+        """mesh.go:80-103 on the GPU: each corner's normal becomes the normalised
+        sum, in corner order, of the normals at the same position whose dot
+        product with it is at least cos(radians)."""
+        from .meshops import DeviceMesh
+        d = DeviceMesh.upload(Mesh(self.tri_pos, self.tri_nrm if self.tri_nrm is not None
+                                   else np.zeros_like(self.tri_pos)))
+        d.SmoothNormalsThreshold(radians)
+        self.tri_nrm = d.download().tri_nrm
         self.dirty()
 
     def SmoothNormals(self):
-        """mesh.go:105-120: per position, the normalised sum of all its normals."""
-        nrm = (self.tri_nrm if self.tri_nrm is not None else np.zeros_like(self.tri_pos)).reshape(-1, 3)
-        inv, order, starts, counts = self._position_groups()
-        sums = np.zeros((counts.size, 3))
-        gmax = int(counts.max()) if counts.size else 0
-        member = np.full((counts.size, gmax), -1, dtype=np.int64)
-        rank = np.arange(order.size) - np.repeat(starts, counts)
-        member[inv[order], rank] = order
-        for k in range(gmax):
-            idx = member[:, k]
-            valid = idx >= 0
-            sums = sums + np.where(valid[:, None], nrm[np.where(valid, idx, 0)], 0.0)
-        self.tri_nrm = _normalize(sums)[inv].reshape(-1, 3, 3)
+        """mesh.go:105-120 on the GPU: per position, the normalised sum of all its normals."""
+        from .meshops import DeviceMesh
+        d = DeviceMesh.upload(Mesh(self.tri_pos, self.tri_nrm if self.tri_nrm is not None
+                                   else np.zeros_like(self.tri_pos)))
+        d.SmoothNormals()
+        self.tri_nrm = d.download().tri_nrm
         self.dirty()
+
+    def SharpEdges(self, angle_threshold):
+        """mesh.go:258-292 on the GPU: a line Mesh of the edges whose two faces
+        meet at more than angle_threshold radians."""
+        from .meshops import DeviceMesh
+        return DeviceMesh.upload(Mesh(self.tri_pos)).SharpEdges(angle_threshold).download()
+
+    def Silhouette(self, eye, offset):
+        """mesh.go:207-209 / silhouette.go:3-53 on the GPU: a line Mesh."""
+        from .meshops import DeviceMesh
+        src = Mesh(self.tri_pos, self.tri_nrm if self.tri_nrm is not None else np.zeros_like(self.tri_pos))
+        return DeviceMesh.upload(src).Silhouette(eye, offset).download()
+
+
+def _position_groups(mesh):
+    """Group corners by Position as Go's map[Vector] does (== on float64,
+    so -0 and +0 are one key; a NaN position is never found). Returns (inv,
+    order, starts, counts, nan) where order lists corner indices grouped by
+    key, each group in corner (triangle, then V1..V3) order."""
+    p = mesh.tri_pos.reshape(-1, 3) + 0.0  # -0 -> +0
+    nan = np.isnan(p).any(axis=1)
+    inv = group_rows(p)
+    order = np.argsort(inv, kind="stable")
+    counts = np.bincount(inv)
+    starts = np.concatenate([[0], np.cumsum(counts)[:-1]])
+    return inv, order, starts, counts, nan
+
+
+def smooth_normals_threshold_host(mesh, radians):
+    """Host restatement of SmoothNormalsThreshold (mesh.go:80-103), for
+    synthesising meshes without the library: the same bits as the GPU's."""
+    threshold = math.cos(radians)
+    nrm = (mesh.tri_nrm if mesh.tri_nrm is not None else np.zeros_like(mesh.tri_pos)).reshape(-1, 3)
+    inv, order, starts, counts, nan = _position_groups(mesh)
+    gmax = int(counts.max()) if counts.size else 0
+    member = np.full((counts.size, gmax), -1, dtype=np.int64)
+    rank = np.arange(order.size) - np.repeat(starts, counts)
+    member[inv[order], rank] = order
+    acc = np.zeros_like(nrm)
+    mine = nrm
+    for k in range(gmax):
+        idx = member[inv, k]
+        valid = idx >= 0
+        x = nrm[np.where(valid, idx, 0)]
+        take = valid & (_dot(x, mine) >= threshold)
+        # adding +0 for a skipped normal leaves the running sum unchanged:
+        # the sum starts at +0 and is never -0
+        acc = acc + np.where(take[:, None], x, 0.0)
+    acc[nan] = 0.0  # a NaN key finds no normals: the zero vector (normalises to NaN)
+    mesh.tri_nrm = _normalize(acc).reshape(-1, 3, 3)
+    mesh.dirty()
+
+
+def smooth_normals_host(mesh):
+    """Host restatement of SmoothNormals (mesh.go:105-120)."""
+    nrm = (mesh.tri_nrm if mesh.tri_nrm is not None else np.zeros_like(mesh.tri_pos)).reshape(-1, 3)
+    inv, order, starts, counts, nan = _position_groups(mesh)
+    sums = np.zeros((counts.size, 3))
+    gmax = int(counts.max()) if counts.size else 0
+    member = np.full((counts.size, gmax), -1, dtype=np.int64)
+    rank = np.arange(order.size) - np.repeat(starts, counts)
+    member[inv[order], rank] = order
+    for k in range(gmax):
+        idx = member[:, k]
+        valid = idx >= 0
+        sums = sums + np.where(valid[:, None], nrm[np.where(valid, idx, 0)], 0.0)
+    out = _normalize(sums)[inv]
+    out[nan] = 0.0  # a NaN key's lookup finds nothing: the zero Vector
+    mesh.tri_nrm = out.reshape(-1, 3, 3)
+    mesh.dirty()
 
 
 def NewTriangleMesh(tri_pos, tri_nrm=None, tri_tex=None, tri_col=None):

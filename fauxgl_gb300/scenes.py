@@ -17,7 +17,7 @@ import math
 import numpy as np
 
 from .geom import HexColor, LookAt, Perspective, Radians, V, Vector
-from .mesh import Mesh, _normalize, face_normals, group_rows
+from .mesh import Mesh, _normalize, face_normals, group_rows, smooth_normals_threshold_host
 from .shapes import cylinder_segments, sphere_positions
 
 EYE = V(-3, 1, -0.75)
@@ -101,7 +101,7 @@ def displaced_sphere(detail=8, seed=1, smooth_degrees=30.0):
     mesh.BiUnitCube()
     fn = face_normals(mesh.tri_pos)
     mesh.tri_nrm = np.ascontiguousarray(np.repeat(fn[:, None, :], 3, axis=1))
-    mesh.SmoothNormalsThreshold(Radians(smooth_degrees))
+    smooth_normals_threshold_host(mesh, Radians(smooth_degrees))
     return mesh
 
 
@@ -133,7 +133,7 @@ def thumbnail_batch(nmeshes=256, views_per_mesh=4, seed=3, tri_min=200, tri_max=
             m.BiUnitCube()
             fn = face_normals(m.tri_pos)
             m.tri_nrm = np.ascontiguousarray(np.repeat(fn[:, None, :], 3, axis=1))
-            m.SmoothNormalsThreshold(Radians(30.0))
+            smooth_normals_threshold_host(m, Radians(30.0))
         else:
             seg = int(math.exp(math.log(8) + rng.uniform() * (math.log(512) - math.log(8))))
             m = cylinder_segments(seg, capped=True, cone=(kind == 2))

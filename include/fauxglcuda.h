@@ -27,6 +27,14 @@
  *   fgc_depth_image         Context.DepthImage             context.go:87-117
  *   fgc_downsample          (no reference counterpart: the examples call the third-party
  *                           resize.Resize after Image(), README.md:107-109)
+ *   fgc_mesh_load_stl       LoadSTL                        stl.go:23-154 (+ Triangle.Normal,
+ *                                                          triangle.go:33-37)
+ *   fgc_mesh_smooth_normals_threshold  Mesh.SmoothNormalsThreshold  mesh.go:80-103
+ *   fgc_mesh_smooth_normals            Mesh.SmoothNormals           mesh.go:105-120
+ *   fgc_mesh_sharp_edges               Mesh.SharpEdges              mesh.go:258-292
+ *   fgc_mesh_silhouette                Mesh.Silhouette              mesh.go:207-209,
+ *                                                                   silhouette.go:3-53
+ *   fgc_mesh_download       the Triangles / Lines of a Mesh (mesh.go:9-13), read back
  *
  * Draw state (fgc_state) mirrors the public Context fields (context.go:40-58);
  * shader parameters (fgc_shader) mirror SolidColorShader / TextureShader /
@@ -163,6 +171,30 @@ int fgc_mesh_upload(const double* tri_pos, const double* tri_nrm, const double* 
                     const double* line_col, uint64_t nline, fgc_mesh** out);
 int fgc_mesh_release(fgc_mesh* mesh);
 int fgc_mesh_counts(const fgc_mesh* mesh, uint64_t* ntri, uint64_t* nline);
+
+/* Mesh preparation on the device. Positions, normals and the position
+ * grouping of the reference's map[Vector] (== on float64: -0 and +0 are one
+ * key, a NaN position is never found) are computed with the reference's
+ * FP64 operation order, so results are the reference's bits; SharpEdges
+ * compares CUDA's acos with the threshold, which may decide differently from
+ * Go's math.Acos for an angle within an ulp or two of it.
+ *
+ * fgc_mesh_load_stl: the bytes of an STL file. Binary when its size is
+ * 84 + 50 * (the header's triangle count), else ASCII ("vertex x y z" lines,
+ * three per triangle). Positions are the file's (FP32 widened to FP64 for
+ * binary); every corner's normal is the triangle's Normal().
+ * fgc_mesh_smooth_normals_threshold / _smooth_normals replace the triangle
+ * corners' normals in place (call with no draw of the mesh in flight).
+ * fgc_mesh_sharp_edges / fgc_mesh_silhouette create a line mesh (release it
+ * with fgc_mesh_release); the input is not changed.
+ * fgc_mesh_download copies positions and normals (3 doubles per corner) into
+ * any non-null array: tri_* 9 per triangle, line_* 6 per line. */
+int fgc_mesh_load_stl(const void* data, uint64_t nbytes, fgc_mesh** out);
+int fgc_mesh_smooth_normals_threshold(fgc_mesh* mesh, double radians);
+int fgc_mesh_smooth_normals(fgc_mesh* mesh);
+int fgc_mesh_sharp_edges(const fgc_mesh* mesh, double angle_threshold, fgc_mesh** out);
+int fgc_mesh_silhouette(const fgc_mesh* mesh, const double eye[3], double offset, fgc_mesh** out);
+int fgc_mesh_download(const fgc_mesh* mesh, double* tri_pos, double* tri_nrm, double* line_pos, double* line_nrm);
 
 /* ImageTexture: texels as the 16-bit alpha-premultiplied RGBA that
  * image.Image.At(x, y).RGBA() returns, row-major, width*height*4 values.

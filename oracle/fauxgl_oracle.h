@@ -68,7 +68,18 @@ void oracle_nrgba(const double c[4], uint8_t out[4]);
 void oracle_blend(uint8_t dst[4], const double src[4]);
 int oracle_clip_triangle(const double clip[12], double out_clip[7 * 3 * 4]);
 
+/* Mesh preparation (fauxgl_oracle_mesh.c): stl.go, mesh.go:80-120, 258-292,
+ * silhouette.go. Lines are 6 doubles (two points); counts beyond cap are
+ * returned but not written. */
+int64_t oracle_stl_parse(const uint8_t* data, uint64_t n, double* tri_pos, double* tri_nrm, uint64_t cap);
+void oracle_smooth_normals_threshold(const double* tri_pos, double* tri_nrm, uint64_t ntri, double threshold);
+void oracle_smooth_normals(const double* tri_pos, double* tri_nrm, uint64_t ntri);
+int64_t oracle_sharp_edges(const double* tri_pos, uint64_t ntri, double angle_threshold, double* out, uint64_t cap);
+int64_t oracle_silhouette(const double* tri_pos, const double* tri_nrm, uint64_t ntri, const double eye[3],
+                          double offset, double* out, uint64_t cap);
+
 #ifdef __cplusplus
 }
 #endif
+
 #endif

@@ -59,6 +59,15 @@ def load():
     lib.oracle_blend.argtypes = [U8, D]
     lib.oracle_clip_triangle.restype = ctypes.c_int
     lib.oracle_clip_triangle.argtypes = [D, D]
+    U64 = ctypes.c_uint64
+    lib.oracle_stl_parse.restype = ctypes.c_int64
+    lib.oracle_stl_parse.argtypes = [U8, U64, D, D, U64]
+    lib.oracle_smooth_normals_threshold.argtypes = [D, D, U64, ctypes.c_double]
+    lib.oracle_smooth_normals.argtypes = [D, D, U64]
+    lib.oracle_sharp_edges.restype = ctypes.c_int64
+    lib.oracle_sharp_edges.argtypes = [D, U64, ctypes.c_double, D, U64]
+    lib.oracle_silhouette.restype = ctypes.c_int64
+    lib.oracle_silhouette.argtypes = [D, D, U64, D, ctypes.c_double, D, U64]
     _lib = lib
     return lib
 
@@ -178,3 +187,62 @@ def clip_triangle(clip):
     out = np.zeros(7 * 3 * 4)
     n = load().oracle_clip_triangle(_d(c), _d(out))
     return out.reshape(7, 3, 4)[:n].copy()
+
+
+# ---------------------------------------------------------------------------
+# mesh preparation (fauxgl_oracle_mesh.c)
+# ---------------------------------------------------------------------------
+def stl_parse(data):
+    """LoadSTL on bytes: (tri_pos (T,3,3), tri_nrm (T,3,3)); raises ValueError
+    where the reference errors."""
+    lib = load()
+    buf = np.frombuffer(bytes(data), dtype=np.uint8)
+    ptr = buf.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+    n = lib.oracle_stl_parse(ptr, buf.size, None, None, 0)
+    if n < 0:
+        raise ValueError("not an STL file the reference reads (%d)" % n)
+    pos = np.zeros((max(n, 1), 3, 3))
+    nrm = np.zeros((max(n, 1), 3, 3))
+    lib.oracle_stl_parse(ptr, buf.size, _d2(pos), _d2(nrm), n)
+    return pos[:n], nrm[:n]
+
+
+def _d2(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def smooth_normals_threshold(tri_pos, tri_nrm, threshold):
+    """Mesh.SmoothNormalsThreshold with threshold = cos(radians) given."""
+    pos = np.ascontiguousarray(tri_pos, dtype=np.float64)
+    nrm = np.ascontiguousarray(tri_nrm, dtype=np.float64).copy()
+    load().oracle_smooth_normals_threshold(_d2(pos), _d2(nrm), pos.shape[0], float(threshold))
+    return nrm
+
+
+def smooth_normals(tri_pos, tri_nrm):
+    pos = np.ascontiguousarray(tri_pos, dtype=np.float64)
+    nrm = np.ascontiguousarray(tri_nrm, dtype=np.float64).copy()
+    load().oracle_smooth_normals(_d2(pos), _d2(nrm), pos.shape[0])
+    return nrm
+
+
+def sharp_edges(tri_pos, angle_threshold):
+    """Mesh.SharpEdges: line positions (L, 2, 3) in the reference's order."""
+    lib = load()
+    pos = np.ascontiguousarray(tri_pos, dtype=np.float64)
+    n = lib.oracle_sharp_edges(_d2(pos), pos.shape[0], float(angle_threshold), None, 0)
+    out = np.zeros((max(n, 1), 2, 3))
+    lib.oracle_sharp_edges(_d2(pos), pos.shape[0], float(angle_threshold), _d2(out), n)
+    return out[:n]
+
+
+def silhouette(tri_pos, tri_nrm, eye, offset):
+    """Mesh.Silhouette: line positions (L, 2, 3) in the reference's order."""
+    lib = load()
+    pos = np.ascontiguousarray(tri_pos, dtype=np.float64)
+    nrm = np.ascontiguousarray(tri_nrm, dtype=np.float64)
+    e = np.ascontiguousarray(eye, dtype=np.float64)
+    n = lib.oracle_silhouette(_d2(pos), _d2(nrm), pos.shape[0], _d2(e), float(offset), None, 0)
+    out = np.zeros((max(n, 1), 2, 3))
+    lib.oracle_silhouette(_d2(pos), _d2(nrm), pos.shape[0], _d2(e), float(offset), _d2(out), n)
+    return out[:n]

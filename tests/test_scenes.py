@@ -7,7 +7,7 @@ import pytest
 
 from fauxgl_gb300 import scenes
 from fauxgl_gb300.geom import HexColor, LookAt, Perspective, Screen, V, Vector
-from fauxgl_gb300.mesh import Mesh, NewTriangleForPoints
+from fauxgl_gb300.mesh import Mesh, NewTriangleForPoints, smooth_normals_threshold_host
 from fauxgl_gb300.shapes import NewCone, NewCube, NewCylinder, NewIcosahedron, NewSphere, cylinder_segments
 
 
@@ -55,7 +55,7 @@ def test_smooth_normals_threshold_properties():
     m0 = scenes.sphere_scene(2)
     fn = m0.tri_nrm.copy()
     m1 = Mesh(m0.tri_pos, np.repeat(_face(m0.tri_pos)[:, None, :], 3, axis=1))
-    m1.SmoothNormalsThreshold(math.radians(89))
+    smooth_normals_threshold_host(m1, math.radians(89))
     keys = {}
     for p, nn in zip(m1.tri_pos.reshape(-1, 3), m1.tri_nrm.reshape(-1, 3)):
         keys.setdefault(tuple(p), set()).add(tuple(nn))
@@ -74,7 +74,7 @@ def test_smooth_normals_sequential_sum_order():
     p = np.array([[[0, 0, 0], [1, 0, 0], [0, 1, 0]], [[0, 0, 0], [0, 1, 0], [-1, 0, 0]]], dtype=float)
     n = np.array([[[0.1, 0.2, 0.97], [0, 0, 1], [0, 0, 1]], [[0.3, -0.1, 0.95], [0, 0, 1], [0, 0, 1]]])
     m = Mesh(p, n)
-    m.SmoothNormalsThreshold(math.radians(30))
+    smooth_normals_threshold_host(m, math.radians(30))
     a, b = Vector(*n[0, 0]), Vector(*n[1, 0])
     expect = Vector(0, 0, 0).Add(a).Add(b).Normalize()
     assert tuple(m.tri_nrm[0, 0]) == tuple(expect)
