@@ -75,7 +75,7 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per rate of the serving loop")
     ap.add_argument("--serve-max-requests", type=int, default=160, help="requests per rate at most")
     ap.add_argument("--serve-budget-gb", type=int, default=96, help="HBM budget of the serving loop")
-    ap.add_argument("--only", choices=["all", "plain", "mixed", "ss16", "batch", "serve"], default="all",
+    ap.add_argument("--only", choices=["all", "plain", "mixed", "ss16", "batch", "serve", "meshprep"], default="all",
                     help="plain / mixed / ss16 / batch / serve: time only the plain or mixed 1080p frame, the plain "
                          "16x supersampled frame, the thumbnail batch or the serving loop (for profiler runs)")
     return ap.parse_args()
@@ -416,6 +416,73 @@ def bench_batch(lib, args, torch):
     }
 
 
+MESHPREP_WORKLOAD = ("mesh preparation around the draw path on the dense 1,310,720-triangle mesh: LoadSTL of its "
+                     "binary STL (62.9 MB, decode + face normals + weld on the GPU), SmoothNormalsThreshold(30 deg), "
+                     "SmoothNormals, SharpEdges(30 deg), Silhouette(eye, 0.001); host wall time per call (each call "
+                     "synchronises), against the oracle's single-threaded C restatement on the same data")
+
+
+def bench_meshprep(lib, mesh, torch, cpu=True):
+    """The §8(f) mesh-preparation rows, each one library call, timed end to
+    end on the host (median of 5 after 1 warm-up); the oracle's C
+    restatement timed once on the same inputs."""
+    import struct
+    import numpy as np
+    from fauxgl_gb300 import scenes
+    from fauxgl_gb300.meshops import DeviceMesh
+    t0 = time.time()
+    pos32 = np.ascontiguousarray(mesh.tri_pos, dtype="<f4").reshape(-1, 9)
+    rec = np.zeros((mesh.ntri, 50), dtype=np.uint8)
+    rec[:, 12:48] = pos32.view(np.uint8).reshape(-1, 36)
+    data = b"meshprep".ljust(80, b" ") + struct.pack("<I", mesh.ntri) + rec.tobytes()
+    log("meshprep: %d-byte STL built (%.1fs)" % (len(data), time.time() - t0))
+
+    def med(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            t = time.perf_counter()
+            fn()
+            ts.append((time.perf_counter() - t) * 1e3)
+        return round(statistics.median(ts), 3)
+
+    eye = tuple(scenes.EYE)
+    dm = DeviceMesh.load_stl(data)
+    out = {"workload": MESHPREP_WORKLOAD, "triangles": mesh.ntri, "unit": "ms per call (host wall time)"}
+    out["load_stl_ms"] = med(lambda: DeviceMesh.load_stl(data))
+    out["smooth_normals_threshold_ms"] = med(lambda: dm.SmoothNormalsThreshold(scenes.Radians(30.0)))
+    out["smooth_normals_ms"] = med(lambda: dm.SmoothNormals())
+    dm = DeviceMesh.load_stl(data)
+    out["sharp_edges_ms"] = med(lambda: dm.SharpEdges(scenes.Radians(30.0)))
+    out["silhouette_ms"] = med(lambda: dm.Silhouette(eye, 0.001))
+    out["sharp_edges_lines"] = dm.SharpEdges(scenes.Radians(30.0)).nline
+    out["silhouette_lines"] = dm.Silhouette(eye, 0.001).nline
+    out["mtri_per_s"] = {k[:-3]: round(mesh.ntri / v / 1e3, 1) for k, v in list(out.items()) if k.endswith("_ms")}
+    if cpu:
+        from oracle import oracle as O
+        import math
+        c = {}
+        t = time.perf_counter()
+        p, n = O.stl_parse(data)
+        c["load_stl_ms"] = round((time.perf_counter() - t) * 1e3, 1)
+        t = time.perf_counter()
+        O.smooth_normals_threshold(p, n, math.cos(scenes.Radians(30.0)))
+        c["smooth_normals_threshold_ms"] = round((time.perf_counter() - t) * 1e3, 1)
+        t = time.perf_counter()
+        O.smooth_normals(p, n)
+        c["smooth_normals_ms"] = round((time.perf_counter() - t) * 1e3, 1)
+        t = time.perf_counter()
+        O.sharp_edges(p, scenes.Radians(30.0))
+        c["sharp_edges_ms"] = round((time.perf_counter() - t) * 1e3, 1)
+        t = time.perf_counter()
+        O.silhouette(p, n, eye, 0.001)
+        c["silhouette_ms"] = round((time.perf_counter() - t) * 1e3, 1)
+        out["cpu_baseline"] = {"kind": "port", "cores": 1, "unit": "ms per call", **c,
+                               "sample": "the same mesh, once each, oracle C restatement (sorting-based grouping)"}
+    return out
+
+
 SERVE_WORKLOAD = ("serving loop: pool of 64 resident meshes (displaced icospheres, 5k-1.31M triangles log-uniform, "
                   "seed 4), Poisson arrivals, each request a random mesh, camera at radius 3, resolution in "
                   "{512^2, 1920x1080, 3840x2160}, supersampling scale in {1, 2, 4} (box-downsampled on the "
@@ -628,6 +695,9 @@ def main():
     if args.only == "serve":
         print(json.dumps({"serve": bench_serve(args, pool)}), flush=True)
         return 0
+    if args.only == "meshprep":
+        print(json.dumps({"meshprep": bench_meshprep(lib, mesh, torch)}), flush=True)
+        return 0
 
     # ---- headline: plain FP64 at 1080p, mesh resident ------------------------
     # nvidia-smi samples the clocks over all GPU measurements below.
@@ -685,9 +755,11 @@ def main():
                                       "overlay": {k: round(v / n, 3) for k, v in zip(_abi.STAGE_NAMES, f.pass_ms[1])}},
                         "work": {"surface": f.pass_work[0], "overlay": f.pass_work[1]}}
             f.close()
-    batch = serve = None
+    batch = serve = meshprep = None
     if args.only == "all" and args.batch_steps > 0 and single:
         batch = bench_batch(lib, args, torch)
+    if args.only == "all" and single:
+        meshprep = bench_meshprep(lib, mesh, torch, cpu=rank == 0)
     if args.only == "all" and pool is not None:
         serve = bench_serve(args, pool)
     clocks.__exit__(None, None, None)
@@ -757,6 +829,7 @@ def main():
             "ss16": ss,
             "batch": batch,
             "serve": serve,
+            "meshprep": meshprep,
             "clocks": clocks.summary(),
         }
         if cpu is not None:
