@@ -454,8 +454,12 @@ __device__ __forceinline__ double dot4(D4 a, D4 b) {
                      __dmul_rn(a.w, b.w));
 }
 // VectorW.Outside (vector.go:212-215).
+// VectorW.Outside (vector.go:212-215): x < -w || x > w || ... with IEEE
+// comparisons (false for NaN, -0 == +0), evaluated on the integer pipe.
 __device__ __forceinline__ bool outside4(D4 a) {
-    return a.x < -a.w || a.x > a.w || a.y < -a.w || a.y > a.w || a.z < -a.w || a.z > a.w;
+    const double nw = __longlong_as_double(__double_as_longlong(a.w) ^ (long long)0x8000000000000000ull);  // -w
+    return dgt_i(nw, a.x) || dgt_i(a.x, a.w) || dgt_i(nw, a.y) || dgt_i(a.y, a.w) || dgt_i(nw, a.z) ||
+           dgt_i(a.z, a.w);
 }
 
 // Matrix.MulPositionW (matrix.go:216-222).

@@ -237,7 +237,7 @@ __device__ void emit_triangle_piece(const GeomParams& P, const ItemView& I, uint
                     (uint32_t)t);
 }
 
-__global__ void __launch_bounds__(kSetupTile) setup_kernel(GeomParams P) {
+__global__ void __launch_bounds__(kSetupTile, 3) setup_kernel(GeomParams P) {
     __shared__ uint32_t s_tile;
     __shared__ OrderedAllocSmem<kSetupTile> s_alloc;
     __shared__ uint64_t s_slot[kSetupTile];
@@ -436,6 +436,17 @@ __device__ FullVertex load_corner(const GeomParams& P, const ItemView& I, uint64
 // ClipTriangle (clipping.go:54-74) + drawClippedTriangle for each piece.
 // Entry e owns primitive slots [base, base + 7*per) and pool vertices
 // [21e, 21e + 21).
+// One vertex of the clipped polygon as ClipTriangle builds it: barycentric
+// weights of its clip-space point w.r.t. the original triangle, then
+// InterpolateVertexes of Output and of the attributes the shader reads.
+__device__ __forceinline__ FullVertex clip_vertex(const FullVertex* tv, D3 p1, D3 p2, D3 p3, D4 q, uint32_t mask) {
+    const D4 bw = barycentric(p1, p2, p3, d3(q.x, q.y, q.z));
+    FullVertex v;
+    v.out = interp_out(tv[0], tv[1], tv[2], bw);
+    interp_attrs(v, tv[0], tv[1], tv[2], bw, mask);
+    return v;
+}
+
 __global__ void __launch_bounds__(128) clip_triangles_kernel(GeomParams P) {
     uint32_t n = min(*P.clip_count, P.clip_cap);
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
@@ -450,8 +461,13 @@ __global__ void __launch_bounds__(128) clip_triangles_kernel(GeomParams P) {
         D3 p1 = d3(tv[0].out.x, tv[0].out.y, tv[0].out.z);
         D3 p2 = d3(tv[1].out.x, tv[1].out.y, tv[1].out.z);
         D3 p3 = d3(tv[2].out.x, tv[2].out.y, tv[2].out.z);
-        // sutherlandHodgman (clipping.go:28-52)
-        D4 bufa[10], bufb[10];
+        // sutherlandHodgman (clipping.go:28-52). Each plane adds at most one
+        // vertex to a convex polygon (9 after six planes); the buffers hold 16
+        // and drop vertices beyond that, which only a polygon made non-convex
+        // by rounding at several planes could reach. A vertex's side of the
+        // plane is computed once and reused as the next edge's start.
+        constexpr int kPolyMax = 16;
+        D4 bufa[kPolyMax], bufb[kPolyMax];
         bufa[0] = tv[0].out; bufa[1] = tv[1].out; bufa[2] = tv[2].out;
         int nin = 3;
         D4* in = bufa;
@@ -459,59 +475,69 @@ __global__ void __launch_bounds__(128) clip_triangles_kernel(GeomParams P) {
         for (int k = 0; k < 6 && nin > 0; k++) {
             int no = 0;
             D4 s = in[nin - 1];
+            bool sf = point_in_front(k, s);
             for (int j = 0; j < nin; j++) {
-                D4 ev = in[j];
-                if (point_in_front(k, ev)) {
-                    if (!point_in_front(k, s)) out[no++] = intersect_segment(k, s, ev);
-                    out[no++] = ev;
-                } else if (point_in_front(k, s)) {
-                    out[no++] = intersect_segment(k, s, ev);
+                const D4 ev = in[j];
+                const bool ef = point_in_front(k, ev);
+                if (ef) {
+                    if (!sf && no < kPolyMax) out[no++] = intersect_segment(k, s, ev);
+                    if (no < kPolyMax) out[no++] = ev;
+                } else if (sf) {
+                    if (no < kPolyMax) out[no++] = intersect_segment(k, s, ev);
                 }
                 s = ev;
+                sf = ef;
             }
             D4* tmp = in; in = out; out = tmp;
             nin = no;
         }
+        // the fan (0, i-1, i): each polygon vertex is built once and shared by
+        // the pieces that use it; FixNormals acts on each piece's own copies
+        // (NewTriangle of fresh vertices, clipping.go:66-72)
         int sub = 0;
-        for (int i = 2; i < nin && sub < 7; i++, sub++) {
-            D4 bw[3];
-            bw[0] = barycentric(p1, p2, p3, d3(in[0].x, in[0].y, in[0].z));
-            bw[1] = barycentric(p1, p2, p3, d3(in[i - 1].x, in[i - 1].y, in[i - 1].z));
-            bw[2] = barycentric(p1, p2, p3, d3(in[i].x, in[i].y, in[i].z));
-            FullVertex v[3];
-            for (int c = 0; c < 3; c++) v[c].out = interp_out(tv[0], tv[1], tv[2], bw[c]);
-            // drawClippedTriangle (context.go:316-349)
-            D3 n0 = ndc_of(v[0].out), n1 = ndc_of(v[1].out), n2 = ndc_of(v[2].out);
-            int order = cull_decision(I.st, n0.x, n0.y, n1.x, n1.y, n2.x, n2.y);
-            uint64_t slot = base + (uint64_t)sub * per;
-            if (order == 0) {
-                for (int q = 0; q < per; q++) write_dead(P, slot + q);
-                continue;
-            }
-            for (int c = 0; c < 3; c++) interp_attrs(v[c], tv[0], tv[1], tv[2], bw[c], mask);
-            if (mask & kAttrNrm) fix_normals(v[0], v[1], v[2]);  // NewTriangle
-            uint32_t pref[3];
-            for (int c = 0; c < 3; c++) {
-                uint32_t pi = e * 21 + sub * 3 + c;
-                if (mask) {
-                    P.pool[pi] = PoolVertex{v[c].pos.x, v[c].pos.y, v[c].pos.z, v[c].nrm.x, v[c].nrm.y, v[c].nrm.z,
-                                            v[c].tu, v[c].tv, v[c].col.x, v[c].col.y, v[c].col.z, v[c].col.w};
-                    if (I.st.precision == FGC_PRECISION_MIXED)
-                        P.pool32[pi] = PoolVertex32{(float)v[c].pos.x, (float)v[c].pos.y, (float)v[c].pos.z,
-                                                    (float)v[c].nrm.x, (float)v[c].nrm.y, (float)v[c].nrm.z,
-                                                    (float)v[c].tu, (float)v[c].tv, (float)v[c].col.x,
-                                                    (float)v[c].col.y, (float)v[c].col.z, (float)v[c].col.w};
+        if (nin >= 3) {
+            const FullVertex va = clip_vertex(tv, p1, p2, p3, in[0], mask);
+            const D3 na = ndc_of(va.out);
+            FullVertex vb = clip_vertex(tv, p1, p2, p3, in[1], mask);
+            D3 nb = ndc_of(vb.out);
+            for (int i = 2; i < nin && sub < 7; i++, sub++) {
+                const FullVertex vc = clip_vertex(tv, p1, p2, p3, in[i], mask);
+                const D3 nc = ndc_of(vc.out);
+                // drawClippedTriangle (context.go:316-349)
+                const int order = cull_decision(I.st, na.x, na.y, nb.x, nb.y, nc.x, nc.y);
+                const uint64_t slot = base + (uint64_t)sub * per;
+                if (order == 0) {
+                    for (int q = 0; q < per; q++) write_dead(P, slot + q);
+                } else {
+                    FullVertex v[3] = {va, vb, vc};
+                    if (mask & kAttrNrm) fix_normals(v[0], v[1], v[2]);  // NewTriangle
+                    uint32_t pref[3];
+                    for (int c = 0; c < 3; c++) {
+                        uint32_t pi = e * 21 + sub * 3 + c;
+                        if (mask) {
+                            P.pool[pi] = PoolVertex{v[c].pos.x, v[c].pos.y, v[c].pos.z, v[c].nrm.x, v[c].nrm.y,
+                                                    v[c].nrm.z, v[c].tu, v[c].tv, v[c].col.x, v[c].col.y,
+                                                    v[c].col.z, v[c].col.w};
+                            if (I.st.precision == FGC_PRECISION_MIXED)
+                                P.pool32[pi] = PoolVertex32{(float)v[c].pos.x, (float)v[c].pos.y, (float)v[c].pos.z,
+                                                            (float)v[c].nrm.x, (float)v[c].nrm.y, (float)v[c].nrm.z,
+                                                            (float)v[c].tu, (float)v[c].tv, (float)v[c].col.x,
+                                                            (float)v[c].col.y, (float)v[c].col.z, (float)v[c].col.w};
+                        }
+                        pref[c] = kPoolFlag | pi;
+                    }
+                    int i0 = 0, i2 = 2;
+                    if (order < 0) { i0 = 2; i2 = 0; }
+                    D3 nn[3] = {na, nb, nc};
+                    D3 s0 = screen_of_ndc(nn[i0], I.w2, I.h2);
+                    D3 s1 = screen_of_ndc(nn[1], I.w2, I.h2);
+                    D3 s2 = screen_of_ndc(nn[i2], I.w2, I.h2);
+                    emit_triangle(P, I.st, slot, s0, s1, s2, __drcp_rn(v[i0].out.w), __drcp_rn(v[1].out.w),
+                                  __drcp_rn(v[i2].out.w), pref[i0], pref[1], pref[i2], (uint32_t)t);
                 }
-                pref[c] = kPoolFlag | pi;
+                vb = vc;
+                nb = nc;
             }
-            int i0 = 0, i2 = 2;
-            if (order < 0) { i0 = 2; i2 = 0; }
-            D3 nn[3] = {n0, n1, n2};
-            D3 s0 = screen_of_ndc(nn[i0], I.w2, I.h2);
-            D3 s1 = screen_of_ndc(nn[1], I.w2, I.h2);
-            D3 s2 = screen_of_ndc(nn[i2], I.w2, I.h2);
-            emit_triangle(P, I.st, slot, s0, s1, s2, __drcp_rn(v[i0].out.w), __drcp_rn(v[1].out.w),
-                          __drcp_rn(v[i2].out.w), pref[i0], pref[1], pref[i2], (uint32_t)t);
         }
         for (; sub < 7; sub++)
             for (int q = 0; q < per; q++) write_dead(P, base + (uint64_t)sub * per + q);

@@ -426,7 +426,9 @@ int issue_submission(PassScratch& S, cudaStream_t stream, const DevLimits& D, co
         rec.launches++;
         mark(evs, stream);
         if (P.any_tri) {
-            clip_triangles_kernel<<<grid_for(S.clip_cap, 128, D.sms * 4), 128, 0, stream>>>(gp);
+            // one warp per block: a few thousand clip entries still spread over
+            // every SM's FP64 pipes
+            clip_triangles_kernel<<<grid_for(S.clip_cap, 32, D.sms * 8), 32, 0, stream>>>(gp);
             FGC_CUDA(cudaGetLastError());
             rec.launches++;
         }

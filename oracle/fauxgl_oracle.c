@@ -354,11 +354,13 @@ static int sutherland_hodgman(const V4* points, int npoints, V4* out) {
         V4 s = input[nin - 1];
         for (int j = 0; j < nin; j++) {
             V4 e = input[j];
+            /* the buffers hold 16 points (a convex polygon has at most 9);
+             * points beyond are dropped, as on the GPU */
             if (point_in_front(k, e)) {
-                if (!point_in_front(k, s)) output[nout++] = intersect_segment(k, s, e);
-                output[nout++] = e;
+                if (!point_in_front(k, s) && nout < 16) output[nout++] = intersect_segment(k, s, e);
+                if (nout < 16) output[nout++] = e;
             } else if (point_in_front(k, s)) {
-                output[nout++] = intersect_segment(k, s, e);
+                if (nout < 16) output[nout++] = intersect_segment(k, s, e);
             }
             s = e;
         }
@@ -377,7 +379,7 @@ static int clip_triangle(const Vtx* t1, const Vtx* t2, const Vtx* t3, Vtx out[7]
     V4 np[16];
     int n = sutherland_hodgman(pts, 3, np);
     int cnt = 0;
-    for (int i = 2; i < n; i++) {
+    for (int i = 2; i < n && cnt < 7; i++) {  /* the GPU reserves 7 pieces per clipped triangle */
         V4 b1 = barycentric(p1, p2, p3, v3(np[0].x, np[0].y, np[0].z));
         V4 b2 = barycentric(p1, p2, p3, v3(np[i - 1].x, np[i - 1].y, np[i - 1].z));
         V4 b3 = barycentric(p1, p2, p3, v3(np[i].x, np[i].y, np[i].z));
