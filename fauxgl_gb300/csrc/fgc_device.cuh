@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/fauxglcuda.h"
+#include "fgc_intconv.cuh"
 
 namespace fgc {
 
@@ -229,6 +230,9 @@ __device__ __forceinline__ bool dgt0(double x) {
     const unsigned long long b = dbits(x);
     return (b >> 63) == 0 && b != 0 && !bnan(b);
 }
+// x < 0 (NaN and -0: false).
+__device__ __forceinline__ bool dlt0(double x) { return ic_lt0(x); }
+
 // x > y and x <= y exactly as IEEE compares (NaN: false; -0 == +0).
 __device__ __forceinline__ unsigned long long okey0(unsigned long long b) {
     return okey((b & kAbsMask) ? b : 0ull);

@@ -65,17 +65,16 @@ __device__ void make_prim(const GeomParams& P, uint64_t slot, D3 s0, D3 s1, D3 s
         return;
     }
     // integer bounding box (Min/Max, Floor/Ceil, int())
-    double mnx = floor(go_min_i(s0.x, go_min_i(s1.x, s2.x)));
-    double mny = floor(go_min_i(s0.y, go_min_i(s1.y, s2.y)));
-    double mxx = ceil(go_max_i(s0.x, go_max_i(s1.x, s2.x)));
-    double mxy = ceil(go_max_i(s0.y, go_max_i(s1.y, s2.y)));
-    int64_t x0 = go_f2i(mnx), x1 = go_f2i(mxx), y0 = go_f2i(mny), y1 = go_f2i(mxy);
+    const int64_t x0 = go_floor_i(go_min_i(s0.x, go_min_i(s1.x, s2.x)));
+    const int64_t y0 = go_floor_i(go_min_i(s0.y, go_min_i(s1.y, s2.y)));
+    const int64_t x1 = go_ceil_i(go_max_i(s0.x, go_max_i(s1.x, s2.x)));
+    const int64_t y1 = go_ceil_i(go_max_i(s0.y, go_max_i(s1.y, s2.y)));
     const int64_t lim = 1LL << 30;
     if (x1 - x0 > kMaxExtent || y1 - y0 > kMaxExtent || x0 < -lim || x1 > lim || y0 < -lim || y1 > lim) {
         write_dead(P, slot);
         return;
     }
-    D3 p = d3(__dadd_rn((double)x0, 0.5), __dadd_rn((double)y0, 0.5), 0.0);
+    D3 p = d3(__dadd_rn(i2d_i(x0), 0.5), __dadd_rn(i2d_i(y0), 0.5), 0.0);  // |x0|, |y0| <= 2^30 here
     RPrim R;
     R.w0 = edge_fn(s1, s2, p);
     R.w1 = edge_fn(s2, s0, p);
@@ -107,13 +106,13 @@ __device__ void make_prim(const GeomParams& P, uint64_t slot, D3 s0, D3 s1, D3 s
     if (ya > yb) { t = ya; ya = yb; yb = t; t = xa; xa = xb; xb = t; }
     if (yb > yc) { t = yb; yb = yc; yc = t; t = xb; xb = xc; xc = t; }
     if (ya > yb) { t = ya; ya = yb; yb = t; t = xa; xa = xb; xb = t; }
-    double chord = mxx - mnx;
+    double chord = i2d_i(x1 - x0);
     if (yc > ya) {
         const double xl = xa + (yb - ya) / (yc - ya) * (xc - xa);
         chord = fmin(fabs(xb - xl), chord);
     }
     const double span = ceil(chord * (1.0 + 1e-9)) + 4.0;
-    const double bw = (double)(x1 - x0 + 1);
+    const double bw = i2d_i(x1 - x0 + 1);
     P.pspan[slot] = (uint32_t)(span < bw ? span : bw);
 }
 

@@ -467,14 +467,14 @@ __device__ __noinline__ Span row_span(const RPrim& R, const PBox& bx, int32_t y,
     double d0 = __dmul_rn(-w00, R.q0);
     double d1 = __dmul_rn(-w01, R.q1);
     double d2 = __dmul_rn(-w02, R.q2);
-    if (w00 < 0 && d0 > d) d = d0;
-    if (w01 < 0 && d1 > d) d = d1;
-    if (w02 < 0 && d2 > d) d = d2;
-    int64_t di = go_f2i(d);  // d = float64(int(d)); if d < 0 { d = 0 }
+    if (dlt0(w00) && dgt_i(d0, d)) d = d0;
+    if (dlt0(w01) && dgt_i(d1, d)) d = d1;
+    if (dlt0(w02) && dgt_i(d2, d)) d = d2;
+    int64_t di = go_f2i_i(d);  // d = float64(int(d)); if d < 0 { d = 0 }
     if (di < 0) di = 0;
     const int64_t T = (int64_t)bx.x1 - bx.x0 - di;  // steps after the first: x = x0 + d .. x1
     if (T < 0) return sp;
-    d = (double)di;
+    d = i2d_i(di);
     const double ws0 = __dadd_rn(w00, __dmul_rn(R.a0, d));
     const double ws1 = __dadd_rn(w01, __dmul_rn(R.a1, d));
     const double ws2 = __dadd_rn(w02, __dmul_rn(R.a2, d));
@@ -576,13 +576,13 @@ __device__ __forceinline__ uint32_t walk_row(const RPrim& R, const PBox& bx, int
     double d0 = __dmul_rn(-w00, R.q0);
     double d1 = __dmul_rn(-w01, R.q1);
     double d2 = __dmul_rn(-w02, R.q2);
-    if (w00 < 0 && d0 > d) d = d0;
-    if (w01 < 0 && d1 > d) d = d1;
-    if (w02 < 0 && d2 > d) d = d2;
-    int64_t di = go_f2i(d);  // d = float64(int(d)); if d < 0 { d = 0 }
+    if (dlt0(w00) && dgt_i(d0, d)) d = d0;
+    if (dlt0(w01) && dgt_i(d1, d)) d = d1;
+    if (dlt0(w02) && dgt_i(d2, d)) d = d2;
+    int64_t di = go_f2i_i(d);  // d = float64(int(d)); if d < 0 { d = 0 }
     if (di < 0) di = 0;
     if (di > (int64_t)bx.x1 - bx.x0) return 0;  // the row loop starts past x1
-    d = (double)di;
+    d = i2d_i(di);
     double w0 = __dadd_rn(w00, __dmul_rn(R.a0, d));
     double w1 = __dadd_rn(w01, __dmul_rn(R.a1, d));
     double w2 = __dadd_rn(w02, __dmul_rn(R.a2, d));
