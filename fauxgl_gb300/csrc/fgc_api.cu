@@ -86,6 +86,7 @@ int fill_views(const fgc_state* st, const fgc_shader* sh, StateView& sv, ShaderV
         shv.eye32[k] = (float)shv.eye[k];
     }
     shv.power32 = (float)shv.power;
+    shv.power_pos = shv.power > 0 ? 1 : 0;
     shv.object_is_discard = (sh->color[0] == 0 && sh->color[1] == 0 && sh->color[2] == 0 && sh->color[3] == 0);
     if (sh->texture) {
         shv.has_texture = 1;

@@ -118,6 +118,7 @@ struct ShaderView {
     int32_t kind;
     int32_t has_texture;
     int32_t object_is_discard;  // PhongShader: ObjectColor == Discard
+    int32_t power_pos;          // SpecularPower > 0 (the Fragment's test, made once)
     double m[16];
     double color[4];
     double light[3];

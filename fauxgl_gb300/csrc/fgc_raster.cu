@@ -136,7 +136,7 @@ __device__ D4 bilinear64(const TexView& t, double u, double v) {  // texture.go:
     v = __dsub_rn(v, floor(v));
     double x = __dmul_rn(u, (double)(t.w - 1));
     double y = __dmul_rn(v, (double)(t.h - 1));
-    int64_t x0 = go_f2i(x), y0 = go_f2i(y);
+    int64_t x0 = go_f2i_i(x), y0 = go_f2i_i(y);
     int64_t x1 = x0 + 1, y1 = y0 + 1;
     x = __dsub_rn(x, (double)x0);
     y = __dsub_rn(y, (double)y0);
@@ -193,7 +193,7 @@ __device__ D4 shade64(const RasterParams& P, const ItemView& I, const RPrim& R, 
     D4 light = d4(S.ambient[0], S.ambient[1], S.ambient[2], S.ambient[3]);
     double diffuse = go_max0(dot3(nrm, L));
     light = add4(light, muls4(d4(S.diffuse[0], S.diffuse[1], S.diffuse[2], S.diffuse[3]), diffuse));
-    if (dgt0(diffuse) && S.power > 0) {
+    if (dgt0(diffuse) && S.power_pos) {
         D3 camera = normalize3(sub3(d3(S.eye[0], S.eye[1], S.eye[2]), pos));
         D3 negl = d3(-L.x, -L.y, -L.z);
         D3 reflected = sub3(negl, muls3(nrm, __dmul_rn(2.0, dot3(nrm, negl))));  // Reflect, vector.go:175-177
@@ -333,7 +333,7 @@ __device__ float4 shade32(const RasterParams& P, const ItemView& I, const RPrim&
     lr = __fmaf_rn(S.diffuse32[0], diffuse, lr);
     lg = __fmaf_rn(S.diffuse32[1], diffuse, lg);
     lb = __fmaf_rn(S.diffuse32[2], diffuse, lb);
-    if (diffuse > 0 && S.power > 0) {
+    if (diffuse > 0 && S.power_pos) {
         F3 cam = normf3(F3{S.eye32[0] - pos.x, S.eye32[1] - pos.y, S.eye32[2] - pos.z});
         F3 negl = F3{-L.x, -L.y, -L.z};
         float k = 2.0f * dotf3(nrm, negl);
@@ -413,7 +413,7 @@ __device__ __noinline__ int64_t edge_flip(double ws, double a, double q, double 
     // the real-number crossing -ws/a is within a step or two of the exact one
     // (q = 1/a may be infinite for a subnormal a: the estimate then falls
     // outside (lo, hi] and the search starts at lo)
-    const int64_t e = go_f2i(__dmul_rn(-ws, q));
+    const int64_t e = go_f2i_i(__dmul_rn(-ws, q));
     int64_t t = (e > lo + 2 && e - 2 <= hi) ? e - 2 : lo;
     double w;
     if (t > lo) {
