@@ -214,7 +214,7 @@ def test_fractional_specular_power_within_tolerance(gpu_lib):
     assert np.array_equal(p.gpu.Winner(), p.ref.winner())
 
 
-@pytest.mark.parametrize("w,h", [(1, 1), (3, 200), (200, 3), (640, 2), (4100, 9), (61, 37)])
+@pytest.mark.parametrize("w,h", [(1, 1), (3, 200), (200, 3), (640, 2), (4100, 9), (61, 37), (9000, 11), (16000, 5)])
 def test_odd_frame_shapes(gpu_lib, w, h):
     mesh = random_scene(w * 7 + h, ntri=120, nline=30)
     m = scene_matrix(w / h)
