@@ -852,17 +852,30 @@ struct ChunkEntry {
     bool narrow;
 };
 
-__device__ __forceinline__ ChunkEntry chunk_entry(const RasterParams& P, const ItemView& I, const BandCtx& B,
-                                                  uint64_t at, bool box_bound, uint32_t roff) {
+// A bin entry's primitive, box and widest chord, loaded ahead of its chunk.
+struct EntryLoad {
+    uint32_t p, span;
+    PBox box;
+};
+__device__ __forceinline__ EntryLoad load_entry(const RasterParams& P, uint64_t at) {
+    EntryLoad l;
+    l.p = P.bins[at];
+    l.box = P.pbox[l.p];
+    l.span = P.pspan[l.p];
+    return l;
+}
+
+__device__ __forceinline__ ChunkEntry chunk_entry(const ItemView& I, const BandCtx& B, const EntryLoad& l,
+                                                  bool box_bound, uint32_t roff) {
     ChunkEntry c;
-    c.p = P.bins[at];
-    const PBox bx = P.pbox[c.p];
+    c.p = l.p;
+    const PBox bx = l.box;
     rows_in_band(bx, I.W, B, c.ylo, c.nrows);
     c.ylo += (int32_t)roff;  // rows an earlier chunk took
     c.nrows -= (int32_t)roff;
     int64_t wid = (int64_t)bx.x1 - bx.x0 + 1;
     c.narrow = wid <= kNarrow;
-    if (!box_bound && (int64_t)P.pspan[c.p] < wid) wid = P.pspan[c.p];
+    if (!box_bound && (int64_t)l.span < wid) wid = l.span;
     if (wid > B.npx) wid = B.npx;
     if (wid < 0) wid = 0;
     const uint64_t bound = (uint64_t)c.nrows * (uint64_t)wid;
@@ -974,6 +987,8 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
         __syncthreads();
 
         uint64_t k = 0;
+        uint64_t pf_at = ~0ull;  // bin entry (band-relative) whose loads pf holds
+        EntryLoad pf;
         uint32_t roff = 0;  // rows of the entry at k taken by earlier chunks
         int level = 0;      // 0: estimated fragments, 1: widest-chord bound, 2: box bound
         while (k < bcount) {
@@ -996,10 +1011,14 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
             const uint64_t e0 = k + (uint64_t)threadIdx.x * kChunkPer;
             ChunkEntry ce[kChunkPer];
 #pragma unroll
-            for (int j = 0; j < kChunkPer; j++)
-                ce[j] = (e0 + j < bcount)
-                            ? chunk_entry(P, I, B, bstart + e0 + j, level == 2, (e0 + j == k) ? roff : 0u)
-                            : ChunkEntry{0, 0, 0, 0, true};
+            for (int j = 0; j < kChunkPer; j++) {
+                if (e0 + j < bcount) {
+                    const EntryLoad l = (j == 0 && pf_at == e0) ? pf : load_entry(P, bstart + e0 + j);
+                    ce[j] = chunk_entry(I, B, l, level == 2, (e0 + j == k) ? roff : 0u);
+                } else {
+                    ce[j] = ChunkEntry{0, 0, 0, 0, true};
+                }
+            }
             if (threadIdx.x == 0) {
                 const bool dm = ce[0].narrow && ce[0].bound <= (uint32_t)F;
                 // a direct chunk holds at most one unit per thread: a second
@@ -1070,6 +1089,15 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
                     const uint32_t pp = S.cprim[S.uslot[u]];
                     tchunk += walk_row(P.prims[pp], P.pbox[pp], S.urow[u], P, I, B, S, u, &s_nfrag, &s_conflict, vis);
                 }
+                {
+                    // the next chunk's entries load during this one's shading
+                    // and resolve (a redone chunk reloads)
+                    const uint64_t nk = (split ? k : k + nprim) + threadIdx.x;
+                    if (nk < bcount) {
+                        pf = load_entry(P, bstart + nk);
+                        pf_at = nk;
+                    }
+                }
                 __syncthreads();
                 const bool redo = (s_conflict & 2u) != 0;
                 if (redo) {  // nothing was applied: empty the lists, redo with a safer bound
@@ -1115,6 +1143,13 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
                 S.uw1[u] = sp.w1;
                 S.uw2[u] = sp.w2;
                 tot += (uint64_t)sp.cnt;
+            }
+            {
+                const uint64_t nk = (split ? k : k + nprim) + threadIdx.x;  // loads during the rounds
+                if (nk < bcount) {
+                    pf = load_entry(P, bstart + nk);
+                    pf_at = nk;
+                }
             }
             __syncthreads();
             // ---- fragment offsets of the units, in unit order
