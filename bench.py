@@ -86,6 +86,21 @@ def dist_env():
         os.environ.get("LOCAL_RANK", "0"))
 
 
+def reduce_max(values, device):
+    """Max over ranks of each value: N replicas each render their own frames,
+    so the job's step time is the slowest rank's (no data-path collective)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
+def replica_rate(max_ms, world):
+    """Whole-job frames/s of world replicas whose slowest frame takes max_ms."""
+    return world * 1e3 / max_ms
+
+
 def build_scene():
     from fauxgl_gb300 import scenes
     t = time.time()
@@ -793,13 +808,10 @@ def main():
 
     # max over ranks of the per-frame time
     if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms, e2e_ms or 0.0, mixed_ms or 0.0], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t[0])
-        e2e_ms = float(t[1]) if e2e_ms else None
-        mixed_ms = float(t[2]) if mixed_ms else None
-    fps = world * 1e3 / ms
+        ms, e2e_max, mixed_max = reduce_max([ms, e2e_ms or 0.0, mixed_ms or 0.0], "cuda")
+        e2e_ms = e2e_max if e2e_ms else None
+        mixed_ms = mixed_max if mixed_ms else None
+    fps = replica_rate(ms, world)
     if rank == 0:
         out = {
             "metric": METRIC, "value": round(fps, 3), "unit": "frames/s", "n_gpus": world, "steps": args.steps,
