@@ -216,6 +216,7 @@ int mesh_weld_attrs(fgc_mesh* m, cudaStream_t s, int sms, const double* cp, cons
         const uint64_t scan_tiles = (V + 2047) / 2048;
         if (!step(tiles.ensure(scan_tiles + 2), "alloc scan") || !step(cudaMemsetAsync(tiles.p, 0, (scan_tiles + 2) * 8, s), "zero scan")) break;
         ScanParams sp;
+        sp.n_dev = nullptr;
         sp.in = flag.p;
         sp.out = uid.p;
         sp.n = V;

@@ -17,36 +17,17 @@
 //   bin_scatter  per block, warps own consecutive sub-ranges; a stable rank
 //                inside each 32-primitive round comes from comparing band
 //                ranges across lanes, so the output order is the input order.
+#include "fgc_fpjump.cuh"
 #include "fgc_internal.cuh"
 
 namespace fgc {
-
-// The draw's band geometry, as the binning blocks use it.
-struct BandGeom {
-    int32_t W, H, R;
-    uint32_t nbands;
-};
-
-// Bands [bl, bh] that the box's linear index range [y0*W + x0, y1*W + x1],
-// clipped to [0, W*H), meets. Index y*W + x lies in row y + floor(x/W), and
-// band b holds rows [b*R, b*R + R).
-__device__ __forceinline__ bool prim_bands(const BandGeom& G, const PBox& b, uint32_t& bl, uint32_t& bh) {
-    if (b.x0 > b.x1) return false;
-    int64_t rlo = (int64_t)b.y0 + floordiv_w(b.x0, G.W);
-    int64_t rhi = (int64_t)b.y1 + floordiv_w(b.x1, G.W);
-    if (rhi < 0 || rlo > G.H - 1) return false;
-    if (rlo < 0) rlo = 0;
-    if (rhi > G.H - 1) rhi = G.H - 1;
-    bl = (uint32_t)rlo / (uint32_t)G.R;
-    bh = (uint32_t)rhi / (uint32_t)G.R;
-    return true;
-}
 
 constexpr unsigned int kRetryBits = ST_CLIP_OVERFLOW | ST_POOL_OVERFLOW | ST_LOOKBACK_TIMEOUT;
 
 // A binning block's draw and its share [lo, hi) of the draw's primitives.
 struct BinBlock {
     uint32_t item, lblk, nblk;
+    bool row_table;
     uint64_t mat0;
     uint64_t lo, hi;
     BandGeom G;
@@ -60,6 +41,7 @@ __device__ __forceinline__ BinBlock bin_block(const BinParams& P) {
     B.nblk = I.nblk;
     B.mat0 = I.mat0;
     B.G = BandGeom{I.W, I.H, I.R, I.nbands};
+    B.row_table = I.row_table != 0;
     // a failed earlier stage means this pass is re-run: bin nothing
     const bool skip = (*P.status & kRetryBits) != 0;
     const uint64_t p0 = P.iout[B.item].prim_start;
@@ -77,12 +59,70 @@ __global__ void __launch_bounds__(256) bin_count_kernel(BinParams P) {
     for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) hist[i] = 0;
     __syncthreads();
     for (uint64_t p = B.lo + threadIdx.x; p < B.hi; p += blockDim.x) {
-        uint32_t bl, bh;
-        if (prim_bands(B.G, P.pbox[p], bl, bh))
+        uint32_t bl, bh, cnt = 0;
+        const PBox bx = P.pbox[p];
+        if (prim_bands(B.G, bx, bl, bh)) {
             for (uint32_t b = bl; b <= bh; b++) atomicAdd(&hist[b], 1u);
+            if (B.row_table && uses_row_table(bx)) cnt = bh - bl + 1;
+        }
+        P.pnb[p] = cnt;
     }
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) P.mat[B.mat0 + (uint64_t)i * B.nblk + B.lblk] = hist[i];
+}
+
+// Row starts of every (primitive, band) pair: one thread per primitive walks
+// its rows downward, adding b12 per row as rasterize does (context.go:275-277),
+// and records the edge values at its first row in each of its bands (the
+// first row of the box whose index range meets the band, as the raster stage
+// counts them). Gaps above 64 rows are crossed with exact jumps.
+__global__ void __launch_bounds__(256) row_starts_kernel(RowStartParams P) {
+    if (*P.status & (kRetryBits | ST_BIN_OVERFLOW)) return;
+    const uint64_t n = *P.prim_total;
+    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n; p += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t cnt = P.pnb[p];
+        if (cnt == 0) continue;
+        const uint64_t base = P.prs[p];
+        if (base + cnt > P.cap) {
+            atomicOr(P.status, ST_BIN_OVERFLOW);
+            continue;
+        }
+        uint32_t lo = 0, hi = P.nitems - 1;  // the draw holding primitive p
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (P.iout[mid].prim_start <= p) lo = mid;
+            else hi = mid - 1;
+        }
+        const ItemView& I = P.items[lo];
+        const BandGeom G{I.W, I.H, I.R, I.nbands};
+        const PBox bx = P.pbox[p];
+        uint32_t bl, bh;
+        if (!prim_bands(G, bx, bl, bh)) continue;
+        const RPrim& R = P.prims[p];
+        double w0 = R.w0, w1 = R.w1, w2 = R.w2;
+        int64_t cur = bx.y0;
+        for (uint32_t b = bl; b <= bh && b - bl < cnt; b++) {
+            int64_t a = (int64_t)b * I.R - floordiv_w(bx.x1, I.W);
+            if (a < bx.y0) a = bx.y0;
+            const int64_t gap = a - cur;
+            if (gap > 64) {
+                w0 = repeat_add(w0, R.b0, (uint64_t)gap);
+                w1 = repeat_add(w1, R.b1, (uint64_t)gap);
+                w2 = repeat_add(w2, R.b2, (uint64_t)gap);
+            } else {
+                for (int64_t j = 0; j < gap; j++) {
+                    w0 = __dadd_rn(w0, R.b0);
+                    w1 = __dadd_rn(w1, R.b1);
+                    w2 = __dadd_rn(w2, R.b2);
+                }
+            }
+            if (gap > 0) cur = a;
+            double* o = P.rstart + 3 * (base + (b - bl));
+            o[0] = w0;
+            o[1] = w1;
+            o[2] = w2;
+        }
+    }
 }
 
 // Exclusive scan of n uint32 values, 2048 per logical block, single pass.
@@ -94,17 +134,18 @@ __global__ void __launch_bounds__(kScanBlock) scan_u32_kernel(ScanParams P) {
     __shared__ OrderedAllocSmem<kScanBlock> s_alloc;
     const uint32_t tile = block_ticket<kScanBlock>(P.lb, &s_tile);
     const uint64_t base = ((uint64_t)tile * kScanBlock + threadIdx.x) * kScanItems;
+    const uint64_t n = P.n_dev ? min(P.n, (uint64_t)*P.n_dev) : P.n;
     uint32_t v[kScanItems];
     uint64_t sum = 0;
 #pragma unroll
     for (int k = 0; k < kScanItems; k++) {
-        v[k] = (base + k < P.n) ? P.in[base + k] : 0u;
+        v[k] = (base + k < n) ? P.in[base + k] : 0u;
         sum += v[k];
     }
     uint64_t excl = ordered_alloc<kScanBlock>(P.lb, tile, sum, s_alloc);
 #pragma unroll
     for (int k = 0; k < kScanItems; k++) {
-        if (base + k < P.n) P.out[base + k] = (uint32_t)excl;
+        if (base + k < n) P.out[base + k] = (uint32_t)excl;
         excl += v[k];
     }
 }

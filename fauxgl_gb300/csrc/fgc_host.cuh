@@ -157,7 +157,7 @@ struct PassCounters {
     unsigned int band_counter;
     unsigned int tick_setup;
     unsigned int tick_scan;
-    unsigned int pad0;
+    unsigned int tick_rscan;
     unsigned long long prim_total;
     unsigned long long pair_total;
     unsigned long long reserved;
@@ -198,6 +198,8 @@ struct PassScratch {
     DevBuf<PoolVertex> pool;
     DevBuf<PoolVertex32> pool32;
     DevBuf<uint32_t> mat, off, bins;
+    DevBuf<uint32_t> pnb, prs;     // per primitive: bands it is binned to, first row-start slot
+    DevBuf<double> rstart;         // per (primitive, band): edge values at its first row in the band
     DevBuf<unsigned long long> tiles;
     DevBuf<unsigned char> table;   // item views + lookup starts + per-draw results + counters + status
     DevBuf<double> dbg;

@@ -32,6 +32,7 @@ struct __align__(16) ItemView {
     uint32_t stile0;            // first setup tile: triangle tiles, then line tiles
     uint32_t ntri_tiles, nline_tiles;
     uint32_t attr_mask;         // kAttr* bits the shader reads
+    int32_t row_table;          // tall primitives take their row starts from the row-start table
     int32_t clear_color_pending, clear_depth_pending;
     uint32_t clear_color;
     double clear_depth;
@@ -136,6 +137,47 @@ struct BinParams {
     uint32_t* bins;
     uint64_t bin_cap;
     unsigned int* status;
+    uint32_t* pnb;              // per primitive: bands it is binned to (bin_count writes it)
+};
+
+// The draw's band geometry, as the binning blocks use it.
+struct BandGeom {
+    int32_t W, H, R;
+    uint32_t nbands;
+};
+
+// Bands [bl, bh] that the box's linear index range [y0*W + x0, y1*W + x1],
+// clipped to [0, W*H), meets. Index y*W + x lies in row y + floor(x/W), and
+// band b holds rows [b*R, b*R + R).
+__device__ __forceinline__ bool prim_bands(const BandGeom& G, const PBox& b, uint32_t& bl, uint32_t& bh) {
+    if (b.x0 > b.x1) return false;
+    int64_t rlo = (int64_t)b.y0 + floordiv_w(b.x0, G.W);
+    int64_t rhi = (int64_t)b.y1 + floordiv_w(b.x1, G.W);
+    if (rhi < 0 || rlo > G.H - 1) return false;
+    if (rlo < 0) rlo = 0;
+    if (rhi > G.H - 1) rhi = G.H - 1;
+    bl = (uint32_t)rlo / (uint32_t)G.R;
+    bh = (uint32_t)rhi / (uint32_t)G.R;
+    return true;
+}
+
+// Row starts: for every (primitive, band) bin pair, the three edge values
+// w00, w01, w02 rasterize holds at the primitive's first row in the band,
+// built by stepping each primitive's rows serially (the reference's own
+// w0k += b per row), so the raster stage starts a row a few steps from its
+// band's first row instead of from the primitive's top.
+struct RowStartParams {
+    const ItemOut* iout;
+    const ItemView* items;
+    uint32_t nitems;
+    const RPrim* prims;
+    const PBox* pbox;
+    const uint32_t* pnb;
+    const uint32_t* prs;        // exclusive scan of pnb
+    const unsigned long long* prim_total;
+    uint64_t cap;               // row-start slots (the bin capacity)
+    double* rstart;             // [slot][3]
+    unsigned int* status;
 };
 
 struct ScanParams {
@@ -143,7 +185,13 @@ struct ScanParams {
     uint32_t* out;
     uint64_t n;
     Lookback lb;
+    const unsigned long long* n_dev;  // when set, only the first min(n, *n_dev) values are scanned
 };
+
+// Primitives with boxes at most this many rows tall catch up their rows from
+// the top themselves; taller ones have row starts per band.
+constexpr int32_t kRowTableMinRows = 5;
+__device__ __forceinline__ bool uses_row_table(const PBox& b) { return b.y1 - b.y0 + 1 >= kRowTableMinRows; }
 
 struct RasterParams {
     const ItemView* items;
@@ -165,6 +213,8 @@ struct RasterParams {
     const PoolVertex* pool;
     const PoolVertex32* pool32;
     const float4* rf;
+    const uint32_t* prs;        // first row-start slot of each primitive
+    const double* rstart;       // row starts per (primitive, band)
     unsigned int* band_counter;
     unsigned int* status;
     double* dbg;                // debug scratch: gridDim * F * 4 doubles, or null
@@ -180,6 +230,7 @@ __global__ void prim_ranges_kernel(GeomParams P);
 __global__ void bin_count_kernel(BinParams P);
 __global__ void scan_u32_kernel(ScanParams P);
 __global__ void bin_scatter_kernel(BinParams P, int warps);
+__global__ void row_starts_kernel(RowStartParams P);
 
 // Raster kernel entry points (defined with the kernel in fgc_raster.cu).
 const void* raster_kernel_ptr(int precision);

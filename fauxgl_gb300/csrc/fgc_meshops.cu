@@ -381,6 +381,7 @@ bool scan_u32(Work& W, const uint32_t* in, uint32_t* out, uint64_t n, uint64_t* 
         return true;
     }
     ScanParams sp;
+    sp.n_dev = nullptr;
     sp.in = in;
     sp.out = out;
     sp.n = n;

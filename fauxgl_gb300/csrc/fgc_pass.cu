@@ -68,7 +68,10 @@ struct PassPlan {
     size_t smem = 0;
     int bin_warps = 1;
     uint32_t scan_tiles = 1;
+    bool row_table = false;      // some draw uses the row-start table
 };
+
+constexpr double kRowTablePixelsPerElement = 8.0;
 
 uint64_t ceil_div(uint64_t a, uint64_t b) { return (a + b - 1) / b; }
 
@@ -198,6 +201,12 @@ int plan_pass(const Submission& sub, const std::vector<uint32_t>& idx, const Dev
             if (it.shv.object_is_discard) v.attr_mask |= kAttrCol;
         }
         if (it.shv.has_texture || it.shv.kind == FGC_SHADER_TEXTURE) v.attr_mask |= kAttrTex;
+        // the row-start table pays where primitives are a few rows tall or
+        // more: frames with at least kRowTablePixelsPerElement pixels per
+        // drawn element (1080p of a 1.3 M-triangle mesh is below it)
+        v.row_table = ((double)c->W * c->H >= kRowTablePixelsPerElement * (double)std::max<uint64_t>(it.tc + it.lc, 1))
+                          ? 1 : 0;
+        P.row_table = P.row_table || v.row_table;
         v.clear_color_pending = it.clear_color;
         v.clear_depth_pending = it.clear_depth;
         v.clear_color = it.clear_color_value;
@@ -278,7 +287,8 @@ int plan_submission(PassScratch& S, const DevLimits& D, const PassTuning& T, con
         need_vert = std::max(need_vert, P.nvert + 1);
         need_lines = std::max(need_lines, P.nlines + 1);
         need_mat = std::max(need_mat, P.nmat);
-        need_tiles = std::max<uint64_t>(need_tiles, (uint64_t)P.stiles + P.scan_tiles + 4);
+        need_tiles = std::max<uint64_t>(need_tiles, (uint64_t)P.stiles + P.scan_tiles + 4 +
+                                                        ceil_div(prim_capacity(P, S.clip_cap), 2048) + 2);
         need_dbg = need_dbg || P.debug_shaded;
         need_grid = std::max<uint32_t>(need_grid, std::min<uint32_t>(2 * D.sms, P.nbands));
     }
@@ -298,6 +308,9 @@ int plan_submission(PassScratch& S, const DevLimits& D, const PassTuning& T, con
     FGC_CUDA(S.mat.ensure(need_mat));
     FGC_CUDA(S.off.ensure(need_mat));
     FGC_CUDA(S.bins.ensure(S.bin_cap));
+    FGC_CUDA(S.pnb.ensure(need_prims));
+    FGC_CUDA(S.prs.ensure(need_prims));
+    FGC_CUDA(S.rstart.ensure(3 * S.bin_cap));
     FGC_CUDA(S.tiles.ensure(need_tiles));
     FGC_CUDA(S.table.ensure(TL.total));
     FGC_CUDA(S.host_in.ensure(TL.in_bytes() * plans.size()));
@@ -365,7 +378,9 @@ int issue_submission(PassScratch& S, cudaStream_t stream, const DevLimits& D, co
         memcpy(hst + 3 * (nmax + 1), P.band.data(), (n + 1) * 4);
         FGC_CUDA(cudaMemcpyAsync(dtab + TL.views, hin, TL.in_bytes(), cudaMemcpyHostToDevice, stream));
         FGC_CUDA(cudaMemsetAsync(&dhdr->c, 0, TL.out_bytes(n) - offsetof(PassHeader, c), stream));
-        const uint64_t ntiles = (uint64_t)P.stiles + P.scan_tiles + 4;
+        const uint64_t prim_cap0 = prim_capacity(P, S.clip_cap);
+        const uint64_t rs_tiles = ceil_div(prim_cap0, 2048);
+        const uint64_t ntiles = (uint64_t)P.stiles + P.scan_tiles + 4 + rs_tiles + 2;
         FGC_CUDA(cudaMemsetAsync(S.tiles.p, 0, ntiles * 8, stream));
 
         const ItemView* items = (const ItemView*)(dtab + TL.views);
@@ -376,6 +391,7 @@ int issue_submission(PassScratch& S, cudaStream_t stream, const DevLimits& D, co
         unsigned int* status = &dhdr->status;
         unsigned long long* t_setup = S.tiles.p;
         unsigned long long* t_scan = t_setup + P.stiles + 2;
+        unsigned long long* t_rscan = t_scan + P.scan_tiles + 2;
         const uint64_t prim_cap = prim_capacity(P, S.clip_cap);
 
         mark(evs, stream);
@@ -454,12 +470,14 @@ int issue_submission(PassScratch& S, cudaStream_t stream, const DevLimits& D, co
         bp.bins = S.bins.p;
         bp.bin_cap = S.bin_cap;
         bp.status = status;
+        bp.pnb = S.pnb.p;
         const size_t hist_smem = (size_t)P.max_nbands * 4;
         if (hist_smem > 48 * 1024)
             FGC_CUDA(cudaFuncSetAttribute(bin_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem));
         bin_count_kernel<<<P.nblk, 256, hist_smem, stream>>>(bp);
         FGC_CUDA(cudaGetLastError());
         ScanParams sp;
+        sp.n_dev = nullptr;
         sp.in = S.mat.p;
         sp.out = S.off.p;
         sp.n = P.nmat;
@@ -471,6 +489,33 @@ int issue_submission(PassScratch& S, cudaStream_t stream, const DevLimits& D, co
             FGC_CUDA(cudaFuncSetAttribute(bin_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scat_smem));
         bin_scatter_kernel<<<P.nblk, P.bin_warps * 32, scat_smem, stream>>>(bp, P.bin_warps);
         FGC_CUDA(cudaGetLastError());
+        // row starts per (primitive, band): slots from a scan of the
+        // primitives' band counts
+        if (P.row_table) {
+            ScanParams rsp;
+            rsp.in = S.pnb.p;
+            rsp.out = S.prs.p;
+            rsp.n = prim_cap0;
+            rsp.lb = Lookback{t_rscan, &dc->tick_rscan, status, &dc->reserved};
+            rsp.n_dev = &dc->prim_total;  // bin_count wrote the band counts of these
+            scan_u32_kernel<<<(unsigned)rs_tiles, 256, 0, stream>>>(rsp);
+            FGC_CUDA(cudaGetLastError());
+            RowStartParams rq;
+            rq.iout = iout;
+            rq.items = items;
+            rq.nitems = n;
+            rq.prims = S.prims.p;
+            rq.pbox = S.pbox.p;
+            rq.pnb = S.pnb.p;
+            rq.prs = S.prs.p;
+            rq.prim_total = &dc->prim_total;
+            rq.cap = S.bin_cap;
+            rq.rstart = S.rstart.p;
+            rq.status = status;
+            row_starts_kernel<<<grid_for(prim_cap0, 256, D.sms * 8), 256, 0, stream>>>(rq);
+            FGC_CUDA(cudaGetLastError());
+            rec.launches += 2;
+        }
         rec.launches += 3;
         mark(evs, stream);
 
@@ -495,6 +540,8 @@ int issue_submission(PassScratch& S, cudaStream_t stream, const DevLimits& D, co
         rp.pool = S.pool.p;
         rp.pool32 = S.pool32.p;
         rp.rf = S.rf.p;
+        rp.prs = S.prs.p;
+        rp.rstart = S.rstart.p;
         rp.band_counter = &dc->band_counter;
         rp.status = status;
         rp.dbg = P.debug_shaded ? S.dbg.p : nullptr;

@@ -68,6 +68,7 @@ struct BandCtx {
     int64_t i0;
     int32_t r0, rend;
     int32_t npx;
+    uint32_t band;   // the band's index in its draw
     bool early;      // early depth rejection is valid
 };
 
@@ -375,6 +376,43 @@ __device__ __forceinline__ uint32_t u8_of_unit_f32(float c) {
 constexpr int kNarrow = 32;      // boxes at most this wide are walked row by row
 constexpr int kShortRow = 40;    // rows of at most this many steps are walked plainly
 
+// The edge values w00, w01, w02 rasterize holds at row y of primitive pp
+// (after y - y0 row increments): for a tall primitive its row start in this
+// band (row_starts_kernel), for a short one its top row, advanced by the rows
+// between that row and y -- a few plain adds, exact jumps beyond 64 rows.
+__device__ __forceinline__ void row_start(const RasterParams& P, uint32_t pp, const RPrim& R, const PBox& bx,
+                                          int32_t y, const ItemView& I, const BandCtx& B, double& w00, double& w01,
+                                          double& w02) {
+    int64_t first = bx.y0;
+    if (I.row_table && uses_row_table(bx)) {
+        const BandGeom G{I.W, I.H, I.R, I.nbands};
+        uint32_t bl = 0, bh = 0;
+        prim_bands(G, bx, bl, bh);  // the primitive is binned to this band: bl <= B.band
+        const double* rs = P.rstart + 3 * ((uint64_t)P.prs[pp] + (B.band - bl));
+        w00 = rs[0];
+        w01 = rs[1];
+        w02 = rs[2];
+        first = (int64_t)B.r0 - floordiv_w(bx.x1, I.W);
+        if (first < bx.y0) first = bx.y0;
+    } else {
+        w00 = R.w0;
+        w01 = R.w1;
+        w02 = R.w2;
+    }
+    const int64_t r = (int64_t)y - first;
+    if (r > 64) {
+        w00 = repeat_add(w00, R.b0, (uint64_t)r);
+        w01 = repeat_add(w01, R.b1, (uint64_t)r);
+        w02 = repeat_add(w02, R.b2, (uint64_t)r);
+    } else {
+        for (int64_t j = 0; j < r; j++) {
+            w00 = __dadd_rn(w00, R.b0);
+            w01 = __dadd_rn(w01, R.b1);
+            w02 = __dadd_rn(w02, R.b2);
+        }
+    }
+}
+
 // Row state in 32-bit band-relative coordinates: the pixel at x of row y is
 // band pixel rel + x, rel = (y - r0) * W. For a row that meets the band
 // (rows_in_band) and a box within the setup limits (|coordinates| <= 2^30,
@@ -449,20 +487,16 @@ __device__ __noinline__ int64_t edge_flip(double ws, double a, double q, double 
     return H;
 }
 
-// The covered in-band pixels of row y of a primitive: rasterize's row
-// prologue (row start, skip-ahead d) and its covered interval, clipped to
-// the band. visited counts the pixel steps taken one by one.
-__device__ __noinline__ Span row_span(const RPrim& R, const PBox& bx, int32_t y, int32_t r0, int32_t npx, int32_t W,
-                                      uint64_t& visited) {
+// The covered in-band pixels of row y of a primitive whose row starts w00
+// (after y - y0 row increments) are given: rasterize's skip-ahead d and the
+// covered interval, clipped to the band. visited counts the pixel steps
+// taken one by one.
+__device__ __noinline__ Span row_span(const RPrim& R, const PBox& bx, int32_t y, double w00, double w01, double w02,
+                                      int32_t r0, int32_t npx, int32_t W, uint64_t& visited) {
     Span sp;
     sp.xa = 0;
     sp.cnt = 0;
     sp.w0 = sp.w1 = sp.w2 = 0;
-    // w00 after (y - y0) row increments
-    const uint64_t dy = (uint64_t)(y - bx.y0);
-    const double w00 = repeat_add(R.w0, R.b0, dy);
-    const double w01 = repeat_add(R.w1, R.b1, dy);
-    const double w02 = repeat_add(R.w2, R.b2, dy);
     double d = 0;
     double d0 = __dmul_rn(-w00, R.q0);
     double d1 = __dmul_rn(-w01, R.q1);
@@ -556,22 +590,12 @@ __device__ __noinline__ Span row_span(const RPrim& R, const PBox& bx, int32_t y,
 // y, recording every covered in-band pixel as a fragment. Returns the
 // covered in-band pixels (TotalPixels). A fragment beyond the buffer sets bit
 // 2 of *s_conflict: the chunk's size bound failed and the chunk is redone.
-__device__ __forceinline__ uint32_t walk_row(const RPrim& R, const PBox& bx, int32_t y, const RasterParams& P,
-                                             const ItemView& I, const BandCtx& B, RasterSmem& S, uint32_t unit,
-                                             uint32_t* s_nfrag, uint32_t* s_conflict, uint64_t& visited) {
-    const uint64_t dy = (uint64_t)(y - bx.y0);
-    double w00 = R.w0, w01 = R.w1, w02 = R.w2;
-    if (dy <= 64) {
-        for (uint64_t j = 0; j < dy; j++) {  // w00 += b12 at the end of each earlier row
-            w00 = __dadd_rn(w00, R.b0);
-            w01 = __dadd_rn(w01, R.b1);
-            w02 = __dadd_rn(w02, R.b2);
-        }
-    } else {
-        w00 = repeat_add(w00, R.b0, dy);
-        w01 = repeat_add(w01, R.b1, dy);
-        w02 = repeat_add(w02, R.b2, dy);
-    }
+__device__ __forceinline__ uint32_t walk_row(uint32_t pp, const RPrim& R, const PBox& bx, int32_t y,
+                                             const RasterParams& P, const ItemView& I, const BandCtx& B,
+                                             RasterSmem& S, uint32_t unit, uint32_t* s_nfrag, uint32_t* s_conflict,
+                                             uint64_t& visited) {
+    double w00, w01, w02;
+    row_start(P, pp, R, bx, y, I, B, w00, w01, w02);
     double d = 0;
     double d0 = __dmul_rn(-w00, R.q0);
     double d1 = __dmul_rn(-w01, R.q1);
@@ -977,6 +1001,7 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
         B.rend = min(B.r0 + I.R, I.H);
         B.i0 = (int64_t)B.r0 * I.W;
         B.npx = (B.rend - B.r0) * I.W;
+        B.band = band;
         B.early = I.st.read_depth && (!I.st.write_depth || I.st.depth_bias >= 0);
         const int npx = B.npx;
         for (int j = threadIdx.x; j < npx; j += blockDim.x) {
@@ -1087,7 +1112,8 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
                 uint64_t tchunk = 0;
                 for (uint32_t u = threadIdx.x; u < nunit; u += blockDim.x) {
                     const uint32_t pp = S.cprim[S.uslot[u]];
-                    tchunk += walk_row(P.prims[pp], P.pbox[pp], S.urow[u], P, I, B, S, u, &s_nfrag, &s_conflict, vis);
+                    tchunk += walk_row(pp, P.prims[pp], P.pbox[pp], S.urow[u], P, I, B, S, u, &s_nfrag, &s_conflict,
+                                       vis);
                 }
                 {
                     // the next chunk's entries load during this one's shading
@@ -1136,7 +1162,11 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
             // ---- spans: each unit's covered in-band pixels
             for (uint32_t u = threadIdx.x; u < nunit; u += blockDim.x) {
                 const uint32_t pp = S.cprim[S.uslot[u]];
-                const Span sp = row_span(P.prims[pp], P.pbox[pp], S.urow[u], B.r0, B.npx, I.W, vis);
+                const RPrim& R = P.prims[pp];
+                const PBox bx = P.pbox[pp];
+                double w00, w01, w02;
+                row_start(P, pp, R, bx, S.urow[u], I, B, w00, w01, w02);
+                const Span sp = row_span(R, bx, S.urow[u], w00, w01, w02, B.r0, B.npx, I.W, vis);
                 S.ux[u] = sp.xa;
                 S.ucnt[u] = (uint32_t)sp.cnt;
                 S.uw0[u] = sp.w0;
