@@ -87,7 +87,8 @@ __device__ void make_prim(const GeomParams& P, uint64_t slot, D3 s0, D3 s1, D3 s
     double b20 = __dsub_rn(s2.x, s0.x);
     R.a0 = a12; R.a1 = a20; R.a2 = a01;
     R.b0 = b12; R.b1 = b20; R.b2 = b01;
-    R.ra = __drcp_rn(edge_fn(s0, s1, s2));  // 1 / x, correctly rounded
+    const double area2 = edge_fn(s0, s1, s2);
+    R.ra = __drcp_rn(area2);  // 1 / x, correctly rounded
     R.q0 = __drcp_rn(a12);
     R.q1 = __drcp_rn(a20);
     R.q2 = __drcp_rn(a01);
@@ -100,20 +101,22 @@ __device__ void make_prim(const GeomParams& P, uint64_t slot, D3 s0, D3 s1, D3 s
     P.rf[slot] = make_float4((float)r0, (float)r1, (float)r2, 0.0f);
     // A row's covered pixel centres lie on one horizontal chord of the
     // triangle, so a row holds at most (widest chord) + 1 of them; +3 more
-    // cover rounding at both ends and in this estimate. The raster stage
-    // sizes its fragment chunks with this bound (and checks it).
-    double ya = s0.y, yb = s1.y, yc = s2.y, xa = s0.x, xb = s1.x, xc = s2.x, t;
-    if (ya > yb) { t = ya; ya = yb; yb = t; t = xa; xa = xb; xb = t; }
-    if (yb > yc) { t = yb; yb = yc; yc = t; t = xb; xb = xc; xc = t; }
-    if (ya > yb) { t = ya; ya = yb; yb = t; t = xa; xa = xb; xb = t; }
-    double chord = i2d_i(x1 - x0);
-    if (yc > ya) {
-        const double xl = xa + (yb - ya) / (yc - ya) * (xc - xa);
-        chord = fmin(fabs(xb - xl), chord);
+    // cover rounding at both ends and in this estimate. The widest chord runs
+    // through the middle vertex and is |2 area| / height, with 2 area =
+    // edge(s0, s1, s2) and height the largest |y difference| (FP32 from
+    // truncated operands, with a relative margin far above their error). The
+    // raster stage sizes its fragment chunks with this bound and redoes a
+    // chunk the bound does not hold for, so it affects speed only.
+    const unsigned long long h01 = dbits(a01) & kAbsMask, h12 = dbits(a12) & kAbsMask, h20 = dbits(a20) & kAbsMask;
+    const unsigned long long hb = h01 > h12 ? (h01 > h20 ? h01 : h20) : (h12 > h20 ? h12 : h20);
+    const uint32_t bw = (uint32_t)(x1 - x0 + 1);
+    uint32_t span = bw;
+    if (hb != 0) {
+        const float chord = f32_trunc_pos(dbits(area2) & kAbsMask) / f32_trunc_pos(hb);
+        const float s = ceilf(chord * (1.0f + 1.0f / 1024.0f)) + 4.0f;
+        if (s < (float)bw) span = (uint32_t)s;
     }
-    const double span = ceil(chord * (1.0 + 1e-9)) + 4.0;
-    const double bw = i2d_i(x1 - x0 + 1);
-    P.pspan[slot] = (uint32_t)(span < bw ? span : bw);
+    P.pspan[slot] = span;
 }
 
 // line (context.go:283-294): a screen-space quad of width LineWidth as two
@@ -147,7 +150,26 @@ __device__ __forceinline__ void clip_plane(int k, D4& p, D4& n) {
     n = d4(axis == 0 ? -s : 0.0, axis == 1 ? -s : 0.0, axis == 2 ? -s : 0.0, 1.0);
 }
 
-__device__ __forceinline__ bool point_in_front(int k, D4 v) {  // clipping.go:16-18
+__device__ __forceinline__ bool finite4(D4 v) { return dfinite(v.x) && dfinite(v.y) && dfinite(v.z) && dfinite(v.w); }
+__device__ __forceinline__ double axis_of(int k, D4 v) { return (k >> 1) == 0 ? v.x : (k >> 1) == 1 ? v.y : v.z; }
+
+// The planes' P and N are zero except on their axis (+-1) and on w (1), so in
+// a dot product with N in the reference's order ((x + y) + z) + w, the terms
+// of the two other axes are signed zeros when their factors are finite.
+// Adding a signed zero to a nonzero partial sum leaves it unchanged, so the
+// dot product equals RN(N_axis * a + b) for the axis and w terms a, b, except
+// possibly in the sign of a zero result. n_dot returns that short form.
+__device__ __forceinline__ double n_dot(int k, double a, double b) {
+    return __dadd_rn((k & 1) ? a : -a, b);  // N_axis = -1 for even k, +1 for odd k (exact products)
+}
+
+// pointInFront (clipping.go:16-18): (v - P).Dot(N) > 0. The sign of a zero
+// does not change "> 0", so finite points take the short form.
+__device__ __forceinline__ bool point_in_front(int k, D4 v) {
+    if (finite4(v)) {
+        const double s = (k & 1) ? -1.0 : 1.0;
+        return dgt0(n_dot(k, __dsub_rn(axis_of(k, v), s), __dsub_rn(v.w, 1.0)));
+    }
     D4 p, n;
     clip_plane(k, p, n);
     return dot4(sub4(v, p), n) > 0;
@@ -236,7 +258,7 @@ __device__ void emit_triangle_piece(const GeomParams& P, const ItemView& I, uint
                     (uint32_t)t);
 }
 
-__global__ void __launch_bounds__(kSetupTile, 3) setup_kernel(GeomParams P) {
+__global__ void __launch_bounds__(kSetupTile, 4) setup_kernel(GeomParams P) {
     __shared__ uint32_t s_tile;
     __shared__ OrderedAllocSmem<kSetupTile> s_alloc;
     __shared__ uint64_t s_slot[kSetupTile];
@@ -334,12 +356,23 @@ __global__ void __launch_bounds__(kSetupTile, 3) setup_kernel(GeomParams P) {
 // ---------------------------------------------------------------------------
 
 __device__ __forceinline__ D4 intersect_segment(int k, D4 v0, D4 v1) {  // clipping.go:20-26
-    D4 p, n;
-    clip_plane(k, p, n);
-    D4 u = sub4(v1, v0);
-    D4 w = sub4(v0, p);
-    double d = dot4(n, u);
-    double nn = -dot4(n, w);
+    const D4 u = sub4(v1, v0);
+    double d = 0, nn = 0;
+    bool full = !(finite4(u) && finite4(v0));
+    if (!full) {
+        // the short form of both dot products (u and w = v0 - P finite); a
+        // zero result takes the full form, where its sign matters
+        const double s = (k & 1) ? -1.0 : 1.0;
+        d = n_dot(k, axis_of(k, u), u.w);
+        nn = -n_dot(k, __dsub_rn(axis_of(k, v0), s), __dsub_rn(v0.w, 1.0));
+        full = (dbits(d) & kAbsMask) == 0 || (dbits(nn) & kAbsMask) == 0;
+    }
+    if (full) {
+        D4 p, n;
+        clip_plane(k, p, n);
+        d = dot4(n, u);
+        nn = -dot4(n, sub4(v0, p));
+    }
     return add4(v0, muls4(u, __ddiv_rn(nn, d)));
 }
 
@@ -478,12 +511,10 @@ __global__ void __launch_bounds__(128) clip_triangles_kernel(GeomParams P) {
             for (int j = 0; j < nin; j++) {
                 const D4 ev = in[j];
                 const bool ef = point_in_front(k, ev);
-                if (ef) {
-                    if (!sf && no < kPolyMax) out[no++] = intersect_segment(k, s, ev);
-                    if (no < kPolyMax) out[no++] = ev;
-                } else if (sf) {
-                    if (no < kPolyMax) out[no++] = intersect_segment(k, s, ev);
-                }
+                // an edge that crosses the plane adds its intersection, then
+                // its end if that is in front
+                if (ef != sf && no < kPolyMax) out[no++] = intersect_segment(k, s, ev);
+                if (ef && no < kPolyMax) out[no++] = ev;
                 s = ev;
                 sf = ef;
             }

@@ -58,6 +58,24 @@ FGC_HD int64_t go_ceil_i(double f) {
     return (ic_gt0(f) && ic_frac(f)) ? t + 1 : t;
 }
 
+// float32 of the bits b of a non-negative finite float64, rounded toward
+// zero: 0 below the smallest normal float32, the largest float32 above it.
+// An operand of estimates, not a conversion of record.
+FGC_HD float f32_trunc_pos(uint64_t b) {
+    const int e = (int)(b >> 52) - 1023 + 127;
+    uint32_t f;
+    if (e <= 0) f = 0u;
+    else if (e >= 255) f = 0x7f7fffffu;
+    else f = ((uint32_t)e << 23) | (uint32_t)((b >> 29) & 0x7fffffu);
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(f);
+#else
+    float r;
+    memcpy(&r, &f, 4);
+    return r;
+#endif
+}
+
 // float64(v), exact for |v| < 2^53.
 FGC_HD double i2d_i(int64_t v) {
     if (v == 0) return 0.0;

@@ -66,37 +66,52 @@ __device__ __forceinline__ uint64_t block_exclusive_scan(uint64_t v, uint64_t* s
 }
 
 // Publish this block's aggregate, look back over predecessors and return the
-// block's exclusive prefix (thread 0 computes; all threads receive it).
+// block's exclusive prefix (warp 0 computes; all threads receive it). The
+// look-back reads a window of 32 predecessors per round, one per lane: the
+// nearest one holding an inclusive prefix ends the walk, and a window whose
+// relevant part still has an unpublished tile is read again.
 template <int BLOCK>
 __device__ __forceinline__ uint64_t lookback_prefix(const Lookback& L, uint32_t tile, uint64_t agg,
                                                     uint64_t* s_prefix) {
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 32) {
+        const uint32_t lane = threadIdx.x;
         uint64_t excl = 0;
         if (tile == 0) {
-            atomicExch(&L.tiles[0], (unsigned long long)(kFlagPre | (agg & kValMask)));
+            if (lane == 0) atomicExch(&L.tiles[0], (unsigned long long)(kFlagPre | (agg & kValMask)));
         } else {
-            atomicExch(&L.tiles[tile], (unsigned long long)(kFlagAgg | (agg & kValMask)));
-            int64_t j = (int64_t)tile - 1;
+            if (lane == 0) atomicExch(&L.tiles[tile], (unsigned long long)(kFlagAgg | (agg & kValMask)));
+            int64_t hi = (int64_t)tile - 1;  // the window is tiles hi, hi-1, ..., hi-31 (lane order)
             uint32_t spins = 0;
-            while (j >= 0) {
-                uint64_t s = *(volatile unsigned long long*)&L.tiles[j];
-                uint64_t flag = s & ~kValMask;
-                if (flag == 0) {
+            for (;;) {
+                const int64_t j = hi - (int64_t)lane;
+                // before tile 0: an inclusive prefix of 0
+                const uint64_t s = j >= 0 ? *(volatile unsigned long long*)&L.tiles[j] : kFlagPre;
+                const uint64_t flag = s & ~kValMask;
+                const uint32_t pre = __ballot_sync(0xffffffffu, flag == kFlagPre);
+                const uint32_t unset = __ballot_sync(0xffffffffu, flag == 0);
+                // lanes up to the nearest inclusive prefix (all 32 when there is none)
+                const uint32_t upto = pre ? ((pre & (0u - pre)) << 1) - 1u : 0xffffffffu;
+                if (unset & upto) {
                     if (++spins > kSpinLimit) {
-                        atomicOr(L.status, ST_LOOKBACK_TIMEOUT);
+                        if (lane == 0) atomicOr(L.status, ST_LOOKBACK_TIMEOUT);
                         break;
                     }
                     __nanosleep(32);
                     continue;
                 }
-                excl += s & kValMask;
-                if (flag == kFlagPre) break;
-                j--;
+                uint64_t v = ((upto >> lane) & 1u) ? (s & kValMask) : 0;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                excl += v;
+                if (pre) break;
+                hi -= 32;
             }
-            atomicExch(&L.tiles[tile], (unsigned long long)(kFlagPre | ((excl + agg) & kValMask)));
+            if (lane == 0) atomicExch(&L.tiles[tile], (unsigned long long)(kFlagPre | ((excl + agg) & kValMask)));
         }
-        if (tile == gridDim.x - 1 && L.total) *L.total = excl + agg;
-        *s_prefix = excl;
+        if (lane == 0) {
+            if (tile == gridDim.x - 1 && L.total) *L.total = excl + agg;
+            *s_prefix = excl;
+        }
     }
     __syncthreads();
     uint64_t r = *s_prefix;

@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
+#include <cfloat>
 #include <cstring>
 #include <initializer_list>
 
@@ -46,6 +47,23 @@ static int check(double f, uint64_t* n) {
     if (fgc::ic_lt0(f) != (f < 0) || fgc::ic_gt0(f) != (f > 0)) {
         printf("sign %a\n", f);
         return 1;
+    }
+    if (std::isfinite(f)) {  // f32_trunc_pos of |f|: toward zero, 0 below FLT_MIN, FLT_MAX above it
+        const double a = std::fabs(f);
+        float want;
+        if (a < (double)FLT_MIN) want = 0.0f;
+        else if (a >= (double)FLT_MAX) want = FLT_MAX;
+        else {
+            want = (float)a;
+            if ((double)want > a) want = std::nextafter(want, 0.0f);
+        }
+        uint64_t ab;
+        memcpy(&ab, &a, 8);
+        const float got = fgc::f32_trunc_pos(ab);
+        if (got != want) {
+            printf("f32_trunc_pos %a: %a vs %a\n", a, (double)got, (double)want);
+            return 1;
+        }
     }
     if (std::isfinite(f) && std::fabs(f) < 9007199254740992.0 && f == std::trunc(f)) {
         const int64_t v = (int64_t)f;
