@@ -7,6 +7,7 @@
 // interface (fgc_batch.cu) runs passes of many draws.
 #include "fgc_host.cuh"
 
+#include <cmath>
 #include <new>
 
 using namespace fgc;
@@ -87,6 +88,9 @@ int fill_views(const fgc_state* st, const fgc_shader* sh, StateView& sv, ShaderV
     }
     shv.power32 = (float)shv.power;
     shv.power_pos = shv.power > 0 ? 1 : 0;
+    shv.pow_yi = 0;
+    if (shv.power >= 2 && shv.power < 9223372036854775808.0 && shv.power == std::trunc(shv.power))
+        shv.pow_yi = (uint64_t)shv.power;
     shv.object_is_discard = (sh->color[0] == 0 && sh->color[1] == 0 && sh->color[2] == 0 && sh->color[3] == 0);
     if (sh->texture) {
         shv.has_texture = 1;

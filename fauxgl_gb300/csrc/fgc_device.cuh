@@ -125,6 +125,7 @@ struct ShaderView {
     double eye[3];
     double ambient[4], diffuse[4], specular[4];
     double power;
+    uint64_t pow_yi;            // SpecularPower when it is an integer in [2, 2^63), else 0
     TexView tex;
     // the same parameters in FP32 for the mixed form (converted once on the
     // host: a conversion from FP64 runs on the FP64 pipe)
@@ -415,6 +416,50 @@ __device__ inline double go_pow(double x, double y) {
     if (ae > 100000) ae = 100000;
     if (ae < -100000) ae = -100000;
     return ldexp(a1, (int)ae);
+}
+
+// Pow(x, SpecularPower) for the Fragment's specular term (x > 0). When the
+// power is an integer yi in [2, 2^63) (classified on the host) and x is a
+// normal number other than 1, math.Pow takes none of its special cases and
+// forms x**yi by repeated squaring of Frexp(x); here Frexp, the "x1 < .5"
+// renormalisation (an exact doubling) and the Ldexp of a normal result act on
+// the exponent bits, and the multiplications are the reference's own. The
+// reference squares once more after the last exponent bit; nothing reads that
+// value, so it is skipped. Everything else goes through go_pow.
+__device__ __forceinline__ double pow_specular(double x, double y, uint64_t yi) {
+    const unsigned long long b = dbits(x);
+    const unsigned long long ex = b >> 52;  // x > 0: no sign bit
+    if (yi == 0 || ex == 0 || ex >= 2047 || b == 0x3ff0000000000000ull) return go_pow(x, y);
+    unsigned long long x1 = (b & 0x000fffffffffffffull) | 0x3fe0000000000000ull;  // in [0.5, 1)
+    int64_t xe = (int64_t)ex - 1022;
+    unsigned long long a1 = 0x3ff0000000000000ull;  // 1.0
+    bool one = true;
+    int64_t ae = 0;
+    for (uint64_t i = yi; i != 0; i >>= 1) {
+        if (xe < -(1 << 12) || (1 << 12) < xe) {
+            ae += xe;
+            break;
+        }
+        if (i & 1) {  // a1 *= x1; 1 * x1 is x1 itself
+            a1 = one ? x1 : dbits(__dmul_rn(__longlong_as_double((long long)a1), __longlong_as_double((long long)x1)));
+            one = false;
+            ae += xe;
+        }
+        if ((i >> 1) == 0) break;
+        const double d1 = __longlong_as_double((long long)x1);
+        x1 = dbits(__dmul_rn(d1, d1));  // in [0.25, 1)
+        xe <<= 1;
+        if (x1 < 0x3fe0000000000000ull) {  // x1 < .5: x1 += x1
+            x1 += 1ull << 52;
+            xe--;
+        }
+    }
+    // Ldexp(a1, ae); a1 is a normal number in (0, 1]
+    const int64_t e = (int64_t)(a1 >> 52) + ae;
+    if (e >= 1 && e <= 2046) return __longlong_as_double((long long)(a1 + ((unsigned long long)ae << 52)));
+    if (ae > 100000) ae = 100000;
+    if (ae < -100000) ae = -100000;
+    return ldexp(__longlong_as_double((long long)a1), (int)ae);
 }
 
 // ---------------------------------------------------------------------------

@@ -200,7 +200,7 @@ __device__ D4 shade64(const RasterParams& P, const ItemView& I, const RPrim& R, 
         D3 reflected = sub3(negl, muls3(nrm, __dmul_rn(2.0, dot3(nrm, negl))));  // Reflect, vector.go:175-177
         double specular = go_max0(dot3(camera, reflected));
         if (dgt0(specular)) {
-            specular = go_pow(specular, S.power);
+            specular = pow_specular(specular, S.power, S.pow_yi);
             light = add4(light, muls4(d4(S.specular[0], S.specular[1], S.specular[2], S.specular[3]), specular));
         }
     }

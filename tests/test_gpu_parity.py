@@ -214,6 +214,23 @@ def test_fractional_specular_power_within_tolerance(gpu_lib):
     assert np.array_equal(p.gpu.Winner(), p.ref.winner())
 
 
+@pytest.mark.parametrize("power", [1.0, 2.0, 3.0, 7.0, 32.0, 33.0, 255.0, 1000.0, 2.0 ** 40, 2.0 ** 63])
+def test_integer_specular_powers_bit_exact(gpu_lib, power):
+    """Integer SpecularPower takes the repeated-squaring path of math.Pow;
+    1000 and 2^40 drive results below the normal range and the exponent
+    guard's early exit, 2^63 is beyond the integer path."""
+    w, h = 64, 48
+    mesh = random_scene(91, ntri=60)
+    m = scene_matrix(w / h)
+    p = Pair(w, h)
+    run_both(p, mesh, state(), phong(m, (0.3, 0.8, 0.5), (0.3, 0.2, 4.5), (0.27, 0.54, 0.4, 1.0), power=power))
+    g, r = p.gpu.ShadedColor(), p.ref.shaded()
+    gn, rn = np.isnan(g), np.isnan(r)
+    assert np.array_equal(gn, rn)
+    assert np.array_equal(np.where(gn, 0.0, g).view(np.uint64), np.where(rn, 0.0, r).view(np.uint64))
+    p.check()
+
+
 @pytest.mark.parametrize("w,h", [(1, 1), (3, 200), (200, 3), (640, 2), (4100, 9), (61, 37), (9000, 11), (16000, 5)])
 def test_odd_frame_shapes(gpu_lib, w, h):
     mesh = random_scene(w * 7 + h, ntri=120, nline=30)
