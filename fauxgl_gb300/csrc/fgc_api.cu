@@ -95,6 +95,7 @@ int fill_views(const fgc_state* st, const fgc_shader* sh, StateView& sv, ShaderV
     if (sh->texture) {
         shv.has_texture = 1;
         shv.tex.texels = sh->texture->texels.p;
+        shv.tex.unit64 = sh->texture->unit64.p;
         shv.tex.w = sh->texture->w;
         shv.tex.h = sh->texture->h;
     }
@@ -548,7 +549,13 @@ int fgc_texture_upload(const uint16_t* rgba16, int32_t width, int32_t height, fg
     t->h = height;
     size_t n = (size_t)width * height;
     cudaError_t e = t->texels.ensure(n);
+    if (e == cudaSuccess) e = t->unit64.ensure(4 * n);
     if (e == cudaSuccess) e = cudaMemcpy(t->texels.p, rgba16, n * sizeof(ushort4), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        fgc::texel_unit_kernel<<<fgc::grid_for(n, 256, 4096), 256>>>(t->texels.p, n, t->unit64.p);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    }
     if (e != cudaSuccess) {
         delete t;
         return fail(FGC_ERR_CUDA, std::string("texture upload: ") + cudaGetErrorString(e));

@@ -110,6 +110,7 @@ struct MeshView {
 // Texture view: 16-bit premultiplied RGBA texels.
 struct TexView {
     const ushort4* texels;
+    const double* unit64;  // per texel the four channels as float64(c) / 0xffff (the FP64 shaders' texel colour)
     int32_t w, h;
 };
 
@@ -221,6 +222,14 @@ __device__ __forceinline__ double go_min1(double x) {
 }
 // x == 0 (either sign).
 __device__ __forceinline__ bool dzero(double x) { return (dbits(x) & kAbsMask) == 0; }
+// 0 + x: x itself except that -0 becomes +0 (a NaN stays a NaN).
+__device__ __forceinline__ double zero_plus(double x) { return dbits(x) == 0x8000000000000000ull ? 0.0 : x; }
+// 2 * x (exact): one more in the exponent of a normal x below the top binade.
+__device__ __forceinline__ double twice(double x) {
+    const unsigned long long b = dbits(x), e = (b >> 52) & 0x7ff;
+    if (e >= 1 && e <= 2045) return __longlong_as_double((long long)(b + (1ull << 52)));
+    return __dmul_rn(2.0, x);
+}
 // x < 1 (NaN: false).
 __device__ __forceinline__ bool dlt1(double x) {
     const unsigned long long b = dbits(x);

@@ -397,7 +397,7 @@ struct FullVertex {
 
 // ((0 + a*bX) + b*bY + c*bZ) * bW for one component (vertex.go:49-79).
 __device__ __forceinline__ double interp1(double a, double b, double c, D4 w) {
-    double n = __dadd_rn(0.0, __dmul_rn(a, w.x));
+    double n = zero_plus(__dmul_rn(a, w.x));
     n = __dadd_rn(n, __dmul_rn(b, w.y));
     n = __dadd_rn(n, __dmul_rn(c, w.z));
     return __dmul_rn(n, w.w);

@@ -110,6 +110,7 @@ struct fgc_texture {
     int device = 0;
     int32_t w = 0, h = 0;
     fgc::DevBuf<ushort4> texels;
+    fgc::DevBuf<double> unit64;  // 4 per texel: the channels as float64(c) / 0xffff
 };
 
 struct fgc_mesh {

@@ -239,6 +239,7 @@ cudaError_t launch_raster(int precision, int grid, int threads, size_t smem, cud
 
 // Helpers of fgc_misc.cu.
 __global__ void fill_u32_kernel(uint32_t* p, uint64_t n, uint32_t v);
+__global__ void texel_unit_kernel(const ushort4* src, uint64_t n, double* dst);
 __global__ void fill_f64_kernel(double* p, uint64_t n, double v);
 __global__ void downsample_kernel(const uint32_t* src, int32_t w, int32_t h, int32_t scale, uint32_t* dst);
 __global__ void depth_minmax_kernel(const double* d, uint64_t n, unsigned long long* lohi);

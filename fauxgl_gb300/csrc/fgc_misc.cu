@@ -14,6 +14,19 @@ __global__ void fill_u32_kernel(uint32_t* p, uint64_t n, uint32_t v) {
         p[i] = v;
 }
 
+// MakeColor of a 16-bit texel (color.go:25-29): float64(c) / 0xffff per
+// channel, once per texture instead of once per bilinear tap.
+__global__ void texel_unit_kernel(const ushort4* src, uint64_t n, double* dst) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const ushort4 p = src[i];
+        const double d = 65535.0;
+        dst[4 * i + 0] = __ddiv_rn((double)p.x, d);
+        dst[4 * i + 1] = __ddiv_rn((double)p.y, d);
+        dst[4 * i + 2] = __ddiv_rn((double)p.z, d);
+        dst[4 * i + 3] = __ddiv_rn((double)p.w, d);
+    }
+}
+
 __global__ void fill_f64_kernel(double* p, uint64_t n, double v) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
         p[i] = v;

@@ -114,7 +114,7 @@ __device__ __forceinline__ D4 fetch_col64(const RasterParams& P, const MeshView&
 
 // ((0 + a*bX) + b*bY + c*bZ) * bW (vertex.go:57-79).
 __device__ __forceinline__ double interp1(double a, double b, double c, D4 w) {
-    double n = __dadd_rn(0.0, __dmul_rn(a, w.x));
+    double n = zero_plus(__dmul_rn(a, w.x));
     n = __dadd_rn(n, __dmul_rn(b, w.y));
     n = __dadd_rn(n, __dmul_rn(c, w.z));
     return __dmul_rn(n, w.w);
@@ -125,10 +125,9 @@ __device__ __forceinline__ double interp1(double a, double b, double c, D4 w) {
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ D4 tex_at64(const TexView& t, int64_t x, int64_t y) {
     if (x < 0 || y < 0 || x >= t.w || y >= t.h) return d4(0, 0, 0, 0);
-    ushort4 p = t.texels[(uint64_t)y * (uint64_t)t.w + (uint64_t)x];
-    const double d = 65535.0;
-    return d4(__ddiv_rn((double)p.x, d), __ddiv_rn((double)p.y, d), __ddiv_rn((double)p.z, d),
-              __ddiv_rn((double)p.w, d));
+    const double2* q = reinterpret_cast<const double2*>(t.unit64 + 4 * ((uint64_t)y * (uint64_t)t.w + (uint64_t)x));
+    const double2 lo = q[0], hi = q[1];
+    return d4(lo.x, lo.y, hi.x, hi.y);
 }
 
 __device__ D4 bilinear64(const TexView& t, double u, double v) {  // texture.go:41-63
@@ -173,7 +172,6 @@ __device__ D4 shade64(const RasterParams& P, const ItemView& I, const RPrim& R, 
     fetch_pn64(P, M, R.v0, p0, n0);
     fetch_pn64(P, M, R.v1, p1, n1);
     fetch_pn64(P, M, R.v2, p2, n2);
-    D3 pos = d3(interp1(p0.x, p1.x, p2.x, w), interp1(p0.y, p1.y, p2.y, w), interp1(p0.z, p1.z, p2.z, w));
     D3 nrm = normalize3(d3(interp1(n0.x, n1.x, n2.x, w), interp1(n0.y, n1.y, n2.y, w), interp1(n0.z, n1.z, n2.z, w)));
     D4 color;
     if (S.object_is_discard) {
@@ -195,9 +193,11 @@ __device__ D4 shade64(const RasterParams& P, const ItemView& I, const RPrim& R, 
     double diffuse = go_max0(dot3(nrm, L));
     light = add4(light, muls4(d4(S.diffuse[0], S.diffuse[1], S.diffuse[2], S.diffuse[3]), diffuse));
     if (dgt0(diffuse) && S.power_pos) {
+        // the interpolated position is read only here
+        const D3 pos = d3(interp1(p0.x, p1.x, p2.x, w), interp1(p0.y, p1.y, p2.y, w), interp1(p0.z, p1.z, p2.z, w));
         D3 camera = normalize3(sub3(d3(S.eye[0], S.eye[1], S.eye[2]), pos));
         D3 negl = d3(-L.x, -L.y, -L.z);
-        D3 reflected = sub3(negl, muls3(nrm, __dmul_rn(2.0, dot3(nrm, negl))));  // Reflect, vector.go:175-177
+        D3 reflected = sub3(negl, muls3(nrm, twice(dot3(nrm, negl))));  // Reflect, vector.go:175-177
         double specular = go_max0(dot3(camera, reflected));
         if (dgt0(specular)) {
             specular = pow_specular(specular, S.power, S.pow_yi);
