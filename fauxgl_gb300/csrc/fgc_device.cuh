@@ -545,9 +545,29 @@ __device__ __forceinline__ D3 screen_of_ndc(D3 n, double w2, double h2) {
 }
 
 // Output.DivScalar(W).Vector() (vector.go:233-235).
-__device__ __forceinline__ D3 ndc_of(D4 o) {
-    return d3(__ddiv_rn(o.x, o.w), __ddiv_rn(o.y, o.w), __ddiv_rn(o.z, o.w));
+// x / w correctly rounded, given y = RN(1 / w). q0 = RN(x y) is within 1.5
+// ulp of x / w; one FMA residual correction makes it a faithful rounding,
+// whose residual x - w q1 is then exact, and the second correction
+// RN(q1 + r1 y) is RN(x / w) by Markstein's theorem (P. Markstein,
+// "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. Res. Dev. 34(1), 1990). The argument assumes no
+// underflow or overflow in any step, which |x| and |w| in [2^-400, 2^401)
+// guarantee; other operands take the division itself.
+// tests/divrcp_check.cu compares it with __ddiv_rn on the GPU.
+__device__ __forceinline__ double div_by_rcp(double x, double w, double y) {
+    const unsigned long long ex = (dbits(x) >> 52) & 0x7ff, ew = (dbits(w) >> 52) & 0x7ff;
+    if (ex - 623ull > 800ull || ew - 623ull > 800ull) return __ddiv_rn(x, w);
+    const double q0 = __dmul_rn(x, y);
+    const double q1 = __fma_rn(__fma_rn(-w, q0, x), y, q0);
+    return __fma_rn(__fma_rn(-w, q1, x), y, q1);
 }
+
+// Output.DivScalar(Output.W).Vector() (vector.go:233-235, context.go:318-320),
+// with y = RN(1 / Output.W).
+__device__ __forceinline__ D3 ndc_of_rcp(D4 o, double y) {
+    return d3(div_by_rcp(o.x, o.w, y), div_by_rcp(o.y, o.w, y), div_by_rcp(o.z, o.w, y));
+}
+__device__ __forceinline__ D3 ndc_of(D4 o) { return ndc_of_rcp(o, __drcp_rn(o.w)); }
 
 // Floor division for possibly negative numerators (b > 0).
 __device__ __forceinline__ int64_t floordiv(int64_t a, int64_t b) {

@@ -29,10 +29,11 @@ __global__ void __launch_bounds__(kVertexTile) vertex_kernel(VertexParams P) {
         const uint64_t o = I.vbase + u;
         P.vclip[o] = VClip{c.x, c.y, c.z, c.w};
         P.vout[o] = outside4(c) ? 1 : 0;
-        D3 n = ndc_of(c);
+        const double rw = __drcp_rn(c.w);
+        D3 n = ndc_of_rcp(c, rw);
         P.vndc[o] = make_double2(n.x, n.y);
         D3 s = screen_of_ndc(n, I.w2, I.h2);
-        P.vscr[o] = VScreen{s.x, s.y, s.z, __drcp_rn(c.w)};
+        P.vscr[o] = VScreen{s.x, s.y, s.z, rw};
     }
 }
 
