@@ -278,6 +278,10 @@ __global__ void __launch_bounds__(kSetupTile, 4) setup_kernel(GeomParams P) {
     uint32_t u0 = 0, u1 = 0, u2 = 0;
     int order = 0;
     bool clip = false;
+    // work: the primitive-emitting pieces this element hands to the packed
+    // FP64 setup below (a triangle, each edge of a wireframe triangle, or a
+    // line); an element that needs clipping instead takes a clip entry
+    uint32_t work = 0;
     if (tri) {
         const int per = I.st.wireframe ? 6 : 1;
         if (valid) {
@@ -298,43 +302,37 @@ __global__ void __launch_bounds__(kSetupTile, 4) setup_kernel(GeomParams P) {
                 order = cull_decision(I.st, n0.x, n0.y, n1.x, n1.y, n2.x, n2.y);
             }
             count = clip ? (uint64_t)(7 * per) : (order != 0 ? (uint64_t)per : 0);
+            if (count != 0 && !clip) work = I.st.wireframe ? 3 : 1;
         }
-    } else {
-        count = valid ? 2 : 0;
+    } else if (valid) {
+        count = 2;
+        const uint64_t cb = 3 * I.mesh.ntri + 2 * (I.line_first + k);
+        u0 = I.mesh.corner_uniq[cb];
+        u1 = I.mesh.corner_uniq[cb + 1];
+        clip = (vout[u0] | vout[u1]) != 0;
+        if (!clip) work = 1;
     }
-    const uint64_t slot = ordered_alloc<kSetupTile>(P.lb, tile, count, s_alloc);
+    uint32_t wpos = 0, nwork = 0;
+    const uint64_t slot = ordered_alloc_pair<kSetupTile>(P.lb, tile, (uint32_t)count, work, s_alloc, wpos, nwork);
     if (lt == 0 && threadIdx.x == 0) P.iout[item].prim_start = slot;  // thread 0's local prefix is 0
 
-    // Clip entries are appended here; the primitive-emitting work (a
-    // triangle, each edge of a wireframe triangle, or a line) is packed onto
-    // consecutive threads so that culled elements leave no idle lanes in the
-    // FP64 setup arithmetic.
-    uint32_t work = 0;
-    if (valid && count != 0) {
+    // Clip entries are appended here; the primitive-emitting work is packed
+    // onto consecutive threads so that culled elements leave no idle lanes in
+    // the FP64 setup arithmetic.
+    if (valid && count != 0 && clip) {
         if (tri) {
-            if (clip) append_clip(P, item, I.tri_first + k, slot);
-            else work = I.st.wireframe ? 3 : 1;
+            append_clip(P, item, I.tri_first + k, slot);
         } else {
-            const uint64_t cb = 3 * I.mesh.ntri + 2 * (I.line_first + k);
-            u0 = I.mesh.corner_uniq[cb];
-            u1 = I.mesh.corner_uniq[cb + 1];
-            if ((vout[u0] | vout[u1]) != 0) {
-                uint32_t idx = atomicAdd(P.lclip_count, 1u);
-                P.lclip_list[idx] = ClipEntry{slot, (uint32_t)(I.line_first + k), item};  // holds every line of the pass
-            } else {
-                work = 1;
-            }
+            uint32_t idx = atomicAdd(P.lclip_count, 1u);
+            P.lclip_list[idx] = ClipEntry{slot, (uint32_t)(I.line_first + k), item};  // holds every line of the pass
         }
     }
-    uint64_t wagg;
-    const uint32_t wpos = (uint32_t)block_exclusive_scan<kSetupTile>(work, s_alloc.warp, &wagg);
     if (work) {
         s_slot[threadIdx.x] = slot;
         s_elem[threadIdx.x] = make_uint4(u0, u1, u2, (uint32_t)order);
         for (uint32_t w = 0; w < work; w++) s_work[wpos + w] = (uint16_t)(threadIdx.x | (w << 8));
     }
     __syncthreads();
-    const uint32_t nwork = (uint32_t)wagg;
     const uint64_t k0 = (uint64_t)(tri ? lt : lt - I.ntri_tiles) * kSetupTile;
     for (uint32_t i = threadIdx.x; i < nwork; i += kSetupTile) {
         const uint32_t j = s_work[i] & 0xFFu, piece = s_work[i] >> 8;

@@ -190,14 +190,20 @@ __device__ D4 shade64(const RasterParams& P, const ItemView& I, const RPrim& R, 
     }
     D3 L = d3(S.light[0], S.light[1], S.light[2]);
     D4 light = d4(S.ambient[0], S.ambient[1], S.ambient[2], S.ambient[3]);
-    double diffuse = go_max0(dot3(nrm, L));
+    const double ndl = dot3(nrm, L);
+    double diffuse = go_max0(ndl);
     light = add4(light, muls4(d4(S.diffuse[0], S.diffuse[1], S.diffuse[2], S.diffuse[3]), diffuse));
     if (dgt0(diffuse) && S.power_pos) {
         // the interpolated position is read only here
         const D3 pos = d3(interp1(p0.x, p1.x, p2.x, w), interp1(p0.y, p1.y, p2.y, w), interp1(p0.z, p1.z, p2.z, w));
         D3 camera = normalize3(sub3(d3(S.eye[0], S.eye[1], S.eye[2]), pos));
         D3 negl = d3(-L.x, -L.y, -L.z);
-        D3 reflected = sub3(negl, muls3(nrm, twice(dot3(nrm, negl))));  // Reflect, vector.go:175-177
+        // Reflect (vector.go:175-177) with n.Dot(-L) = -(n.Dot(L)): rounding is
+        // symmetric, so the two differ at most in the sign of a zero, which
+        // only flips zero signs in `reflected` where -L has a zero component;
+        // those terms add nothing to a nonzero specular dot product and a zero
+        // one fails the "> 0" test either way
+        D3 reflected = sub3(negl, muls3(nrm, twice(-ndl)));
         double specular = go_max0(dot3(camera, reflected));
         if (dgt0(specular)) {
             specular = pow_specular(specular, S.power, S.pow_yi);

@@ -136,4 +136,19 @@ __device__ __forceinline__ uint64_t ordered_alloc(const Lookback& L, uint32_t ti
     return base + local;
 }
 
+// ordered_alloc of `count` that also scans a second per-thread value in the
+// same pass: the two sums share one 64-bit scan (count in the high half,
+// other in the low half; a block's sums of either stay below 2^32).
+template <int BLOCK>
+__device__ __forceinline__ uint64_t ordered_alloc_pair(const Lookback& L, uint32_t tile, uint32_t count, uint32_t other,
+                                                       OrderedAllocSmem<BLOCK>& sm, uint32_t& other_excl,
+                                                       uint32_t& other_total) {
+    uint64_t agg;
+    const uint64_t local = block_exclusive_scan<BLOCK>(((uint64_t)count << 32) | other, sm.warp, &agg);
+    other_excl = (uint32_t)local;
+    other_total = (uint32_t)agg;
+    const uint64_t base = lookback_prefix<BLOCK>(L, tile, agg >> 32, &sm.prefix);
+    return base + (local >> 32);
+}
+
 }  // namespace fgc
