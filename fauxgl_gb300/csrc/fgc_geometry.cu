@@ -222,7 +222,10 @@ __device__ void emit_triangle(const GeomParams& P, const StateView& st, uint64_t
 // triangles, context.go:435-439), and the ordered allocation runs across all
 // of them, so every draw's primitives are one contiguous, ordered range.
 // Triangles take one slot (six in wireframe), or 7x that when they need
-// clipping; lines always take two slots (dead when clipped away).
+// clipping; lines always take two slots (dead when clipped away). setup_kernel
+// decides culling and clipping and allocates; the surviving work items go to
+// a list that setup_emit_kernel turns into raster primitives, while the clip
+// kernels (on another stream) handle the clip entries.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void append_clip(const GeomParams& P, uint32_t item, uint64_t t, uint64_t slot) {
     uint32_t idx = atomicAdd(P.clip_count, 1u);
@@ -259,12 +262,9 @@ __device__ void emit_triangle_piece(const GeomParams& P, const ItemView& I, uint
                     (uint32_t)t);
 }
 
-__global__ void __launch_bounds__(kSetupTile, 4) setup_kernel(GeomParams P) {
+__global__ void __launch_bounds__(kSetupTile) setup_kernel(GeomParams P) {
     __shared__ uint32_t s_tile;
     __shared__ OrderedAllocSmem<kSetupTile> s_alloc;
-    __shared__ uint64_t s_slot[kSetupTile];
-    __shared__ uint4 s_elem[kSetupTile];            // u0, u1, u2, cull order
-    __shared__ uint16_t s_work[3 * kSetupTile];     // element | piece << 8
     const uint32_t tile = block_ticket<kSetupTile>(P.lb, &s_tile);
     const uint32_t item = find_item(P.starts.stile, P.nitems, tile);
     const ItemView& I = P.items[item];
@@ -278,9 +278,9 @@ __global__ void __launch_bounds__(kSetupTile, 4) setup_kernel(GeomParams P) {
     uint32_t u0 = 0, u1 = 0, u2 = 0;
     int order = 0;
     bool clip = false;
-    // work: the primitive-emitting pieces this element hands to the packed
-    // FP64 setup below (a triangle, each edge of a wireframe triangle, or a
-    // line); an element that needs clipping instead takes a clip entry
+    // work: the primitive-emitting pieces this element hands to the emit
+    // kernel (a triangle, each edge of a wireframe triangle, or a line); an
+    // element that needs clipping instead takes a clip entry
     uint32_t work = 0;
     if (tri) {
         const int per = I.st.wireframe ? 6 : 1;
@@ -312,13 +312,13 @@ __global__ void __launch_bounds__(kSetupTile, 4) setup_kernel(GeomParams P) {
         clip = (vout[u0] | vout[u1]) != 0;
         if (!clip) work = 1;
     }
-    uint32_t wpos = 0, nwork = 0;
-    const uint64_t slot = ordered_alloc_pair<kSetupTile>(P.lb, tile, (uint32_t)count, work, s_alloc, wpos, nwork);
+    uint64_t slot, wpos, total;
+    ordered_alloc2<kSetupTile>(P.lb, tile, (uint32_t)count, work, s_alloc, slot, wpos, total);
     if (lt == 0 && threadIdx.x == 0) P.iout[item].prim_start = slot;  // thread 0's local prefix is 0
-
-    // Clip entries are appended here; the primitive-emitting work is packed
-    // onto consecutive threads so that culled elements leave no idle lanes in
-    // the FP64 setup arithmetic.
+    if (tile == gridDim.x - 1 && threadIdx.x == 0) {
+        *P.prim_total = total >> 31;
+        *P.work_total = total & kLow31;
+    }
     if (valid && count != 0 && clip) {
         if (tri) {
             append_clip(P, item, I.tri_first + k, slot);
@@ -327,25 +327,34 @@ __global__ void __launch_bounds__(kSetupTile, 4) setup_kernel(GeomParams P) {
             P.lclip_list[idx] = ClipEntry{slot, (uint32_t)(I.line_first + k), item};  // holds every line of the pass
         }
     }
-    if (work) {
-        s_slot[threadIdx.x] = slot;
-        s_elem[threadIdx.x] = make_uint4(u0, u1, u2, (uint32_t)order);
-        for (uint32_t w = 0; w < work; w++) s_work[wpos + w] = (uint16_t)(threadIdx.x | (w << 8));
+    const uint32_t elem = (uint32_t)((tri ? I.tri_first : I.line_first) + k);
+    const uint32_t meta = (uint32_t)(order + 1) << 8 | (tri ? 0u : kWorkLine);
+    for (uint32_t w = 0; w < work; w++) {
+        if (wpos + w >= P.work_cap) {  // sized for every element: not reached
+            atomicOr(P.status, ST_RASTER_INTERNAL);
+            break;
+        }
+        P.work[wpos + w] = SetupWork{slot, elem, item, u0, u1, u2, meta | w};
     }
-    __syncthreads();
-    const uint64_t k0 = (uint64_t)(tri ? lt : lt - I.ntri_tiles) * kSetupTile;
-    for (uint32_t i = threadIdx.x; i < nwork; i += kSetupTile) {
-        const uint32_t j = s_work[i] & 0xFFu, piece = s_work[i] >> 8;
-        const uint4 e = s_elem[j];
-        if (tri) {
-            emit_triangle_piece(P, I, I.tri_first + k0 + j, s_slot[j], (int)e.w, e.x, e.y, e.z, piece);
-        } else {
-            const uint64_t l = I.line_first + k0 + j;
-            const uint64_t cb = 3 * I.mesh.ntri + 2 * l;
+}
+
+// The FP64 half of setup: one thread per work item, every lane busy (the
+// work list holds only what survived culling), no barriers.
+__global__ void __launch_bounds__(256) setup_emit_kernel(GeomParams P) {
+    const uint64_t n = min((uint64_t)*P.work_total, P.work_cap);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const SetupWork w = P.work[i];
+        const ItemView& I = P.items[w.item];
+        const uint32_t piece = w.meta & 0xFFu;
+        if (w.meta & kWorkLine) {
+            const uint64_t cb = 3 * I.mesh.ntri + 2 * (uint64_t)w.elem;
             const VScreen* vscr = P.vscr + I.vbase;
-            const VScreen a = vscr[e.x], b = vscr[e.y];
-            make_line_prims(P, I.st.line_width, s_slot[j], d3(a.x, a.y, a.z), d3(b.x, b.y, b.z), a.rw, b.rw,
-                            (uint32_t)cb, (uint32_t)(cb + 1), kLineFlag | (uint32_t)l);
+            const VScreen a = vscr[w.u0], b = vscr[w.u1];
+            make_line_prims(P, I.st.line_width, w.slot, d3(a.x, a.y, a.z), d3(b.x, b.y, b.z), a.rw, b.rw,
+                            (uint32_t)cb, (uint32_t)(cb + 1), kLineFlag | w.elem);
+        } else {
+            const int order = (int)((w.meta >> 8) & 0xFFu) - 1;
+            emit_triangle_piece(P, I, w.elem, w.slot, order, w.u0, w.u1, w.u2, piece);
         }
     }
 }

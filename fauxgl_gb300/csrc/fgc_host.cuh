@@ -162,6 +162,8 @@ struct PassCounters {
     unsigned long long prim_total;
     unsigned long long pair_total;
     unsigned long long reserved;
+    unsigned long long work_total;  // setup work items of the pass
+    unsigned long long pad1;
 };
 
 // Tunable shapes of a pass; results do not depend on them.
@@ -204,9 +206,22 @@ struct PassScratch {
     DevBuf<unsigned long long> tiles;
     DevBuf<unsigned char> table;   // item views + lookup starts + per-draw results + counters + status
     DevBuf<double> dbg;
+    DevBuf<SetupWork> work;        // setup work items (triangles, wireframe edges, lines)
     PinnedBuf host_in, host_out;
     uint32_t clip_cap = 1024;
     uint64_t bin_cap = 0;
+    // the clip kernels run on a second stream beside the setup emission
+    int side_device = -1;
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    PassScratch() = default;
+    PassScratch(const PassScratch&) = delete;
+    PassScratch& operator=(const PassScratch&) = delete;
+    ~PassScratch() {
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        if (side) cudaStreamDestroy(side);
+    }
 };
 
 // The host's record of one issued pass (for reading its results).

@@ -79,6 +79,17 @@ __device__ __forceinline__ int32_t floordiv_w(int32_t x, int32_t W) {
 }
 
 // A clipped element: its primitive slots and draw.
+// One primitive-emitting work item of the setup stage: a triangle (slot of
+// its first primitive), one edge of a wireframe triangle, or a line.
+struct __align__(16) SetupWork {
+    uint64_t slot;
+    uint32_t elem;              // triangle or line index in the mesh
+    uint32_t item;              // draw of the pass
+    uint32_t u0, u1, u2;        // unique-vertex indices (u2 unused for lines)
+    uint32_t meta;              // piece | (cull order + 1) << 8 | kWorkLine
+};
+constexpr uint32_t kWorkLine = 1u << 16;
+
 struct __align__(16) ClipEntry {
     unsigned long long slot;    // first primitive slot
     uint32_t elem;              // triangle (or line) index within the mesh
@@ -122,6 +133,9 @@ struct GeomParams {
     unsigned long long* prim_total;
     Lookback lb;
     unsigned int* status;
+    SetupWork* work;            // the primitive-emitting work items, in slot order
+    uint64_t work_cap;
+    unsigned long long* work_total;
 };
 constexpr int kSetupTile = 256;
 
@@ -223,6 +237,7 @@ struct RasterParams {
 // Kernels (grid shapes chosen by the host runtime).
 __global__ void vertex_kernel(VertexParams P);
 __global__ void setup_kernel(GeomParams P);
+__global__ void setup_emit_kernel(GeomParams P);
 __global__ void clip_triangles_kernel(GeomParams P);
 __global__ void clip_lines_kernel(GeomParams P);
 __global__ void prim_ranges_kernel(GeomParams P);

@@ -23,7 +23,7 @@ namespace fgc {
 
 namespace {
 
-constexpr size_t kHeaderBytes = 64;
+constexpr size_t kHeaderBytes = 80;
 
 struct PassHeader {
     unsigned int status;  // submission-wide status word
@@ -69,6 +69,7 @@ struct PassPlan {
     int bin_warps = 1;
     uint32_t scan_tiles = 1;
     bool row_table = false;      // some draw uses the row-start table
+    uint64_t work_items = 0;     // setup work items at most (emitting triangles, wireframe edges, lines)
 };
 
 constexpr double kRowTablePixelsPerElement = 8.0;
@@ -188,6 +189,7 @@ int plan_pass(const Submission& sub, const std::vector<uint32_t>& idx, const Dev
         P.nvert += draws ? it.mesh->nuniq : 0;
         P.nlines += it.lc;
         P.prim_base += prims;
+        P.work_items += it.tc * (it.sv.wireframe ? 3 : 1) + it.lc;
         P.max_nbands = std::max(P.max_nbands, v.nbands);
         P.per_max = std::max(P.per_max, per);
         P.any_tri = P.any_tri || it.tc > 0;
@@ -279,7 +281,7 @@ int plan_submission(PassScratch& S, const DevLimits& D, const PassTuning& T, con
         nmax = std::max<uint32_t>(nmax, (uint32_t)groups[g].size());
     }
     const TableLayout TL = table_layout(nmax);
-    uint64_t need_prims = 0, need_vert = 1, need_lines = 1, need_mat = 1, need_tiles = 4;
+    uint64_t need_prims = 0, need_vert = 1, need_lines = 1, need_mat = 1, need_tiles = 4, need_work = 1;
     bool need_dbg = false;
     need_grid = 1;
     for (const PassPlan& P : plans) {
@@ -291,7 +293,12 @@ int plan_submission(PassScratch& S, const DevLimits& D, const PassTuning& T, con
                                                         ceil_div(prim_capacity(P, S.clip_cap), 2048) + 2);
         need_dbg = need_dbg || P.debug_shaded;
         need_grid = std::max<uint32_t>(need_grid, std::min<uint32_t>(2 * D.sms, P.nbands));
+        need_work = std::max<uint64_t>(need_work, P.work_items);
     }
+    // setup's ordered allocation carries the slot and work prefixes in 31
+    // bits each
+    if (need_prims >= (1ull << 31) || need_work >= (1ull << 31))
+        return fail(FGC_ERR_UNSUPPORTED, "more than 2^31 primitives in one pass");
     if (S.bin_cap == 0) S.bin_cap = std::max<uint64_t>(2 * need_prims, 1 << 16);
     FGC_CUDA(S.vclip.ensure(need_vert));
     FGC_CUDA(S.vndc.ensure(need_vert));
@@ -312,7 +319,25 @@ int plan_submission(PassScratch& S, const DevLimits& D, const PassTuning& T, con
     FGC_CUDA(S.prs.ensure(need_prims));
     FGC_CUDA(S.rstart.ensure(3 * S.bin_cap));
     FGC_CUDA(S.tiles.ensure(need_tiles));
+    FGC_CUDA(S.work.ensure(need_work));
     FGC_CUDA(S.table.ensure(TL.total));
+    int dev = 0;
+    FGC_CUDA(cudaGetDevice(&dev));
+    if (!S.side || S.side_device != dev) {
+        if (S.ev_fork) cudaEventDestroy(S.ev_fork);
+        if (S.ev_join) cudaEventDestroy(S.ev_join);
+        if (S.side) cudaStreamDestroy(S.side);
+        S.side = nullptr;
+        S.ev_fork = S.ev_join = nullptr;
+        // the highest priority: the clip kernel's few blocks are placed before
+        // the emission's fill the SMs
+        int least = 0, greatest = 0;
+        FGC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        FGC_CUDA(cudaStreamCreateWithPriority(&S.side, cudaStreamNonBlocking, greatest));
+        FGC_CUDA(cudaEventCreateWithFlags(&S.ev_fork, cudaEventDisableTiming));
+        FGC_CUDA(cudaEventCreateWithFlags(&S.ev_join, cudaEventDisableTiming));
+        S.side_device = dev;
+    }
     FGC_CUDA(S.host_in.ensure(TL.in_bytes() * plans.size()));
     FGC_CUDA(S.host_out.ensure(TL.out_bytes(nmax) * plans.size()));
     if (need_dbg) {
@@ -435,24 +460,39 @@ int issue_submission(PassScratch& S, cudaStream_t stream, const DevLimits& D, co
         gp.pool = S.pool.p;
         gp.pool32 = S.pool32.p;
         gp.prim_total = &dc->prim_total;
-        gp.lb = Lookback{t_setup, &dc->tick_setup, status, &dc->prim_total};
+        gp.lb = Lookback{t_setup, &dc->tick_setup, status, nullptr};  // setup_kernel writes the totals
         gp.status = status;
+        gp.work = S.work.p;
+        gp.work_cap = S.work.cap;
+        gp.work_total = &dc->work_total;
         setup_kernel<<<P.stiles, kSetupTile, 0, stream>>>(gp);
         FGC_CUDA(cudaGetLastError());
         rec.launches++;
+        // the clip kernels (latency-bound: one long FP64 chain per entry) run
+        // on the side stream while the emission fills every SM's FP64 pipe
+        const bool clips = P.any_tri || P.any_line;
+        if (clips) {
+            FGC_CUDA(cudaEventRecord(S.ev_fork, stream));
+            FGC_CUDA(cudaStreamWaitEvent(S.side, S.ev_fork, 0));
+            if (P.any_tri) {
+                // one warp per block: a few thousand clip entries still spread
+                // over every SM's FP64 pipes
+                clip_triangles_kernel<<<grid_for(S.clip_cap, 32, D.sms * 8), 32, 0, S.side>>>(gp);
+                FGC_CUDA(cudaGetLastError());
+                rec.launches++;
+            }
+            if (P.any_line) {
+                clip_lines_kernel<<<grid_for(P.nlines, 128, D.sms * 4), 128, 0, S.side>>>(gp);
+                FGC_CUDA(cudaGetLastError());
+                rec.launches++;
+            }
+            FGC_CUDA(cudaEventRecord(S.ev_join, S.side));
+        }
+        setup_emit_kernel<<<grid_for(P.work_items, 256, D.sms * 16), 256, 0, stream>>>(gp);
+        FGC_CUDA(cudaGetLastError());
+        rec.launches++;
+        if (clips) FGC_CUDA(cudaStreamWaitEvent(stream, S.ev_join, 0));
         mark(evs, stream);
-        if (P.any_tri) {
-            // one warp per block: a few thousand clip entries still spread over
-            // every SM's FP64 pipes
-            clip_triangles_kernel<<<grid_for(S.clip_cap, 32, D.sms * 8), 32, 0, stream>>>(gp);
-            FGC_CUDA(cudaGetLastError());
-            rec.launches++;
-        }
-        if (P.any_line) {
-            clip_lines_kernel<<<grid_for(P.nlines, 128, D.sms * 4), 128, 0, stream>>>(gp);
-            FGC_CUDA(cudaGetLastError());
-            rec.launches++;
-        }
         prim_ranges_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, stream>>>(gp);
         FGC_CUDA(cudaGetLastError());
         rec.launches++;

@@ -151,4 +151,22 @@ __device__ __forceinline__ uint64_t ordered_alloc_pair(const Lookback& L, uint32
     return base + (local >> 32);
 }
 
+// Ordered allocation of two counts at once: every thread gets the global
+// exclusive prefix of both (a in [0, 2^31) per block and overall, b likewise).
+// They travel packed as a << 31 | b through one block scan and one look-back
+// (L.total must be null); `total` receives the packed inclusive sum of the
+// block, which for the last block is the grand total.
+constexpr uint64_t kLow31 = (1ull << 31) - 1;
+template <int BLOCK>
+__device__ __forceinline__ void ordered_alloc2(const Lookback& L, uint32_t tile, uint32_t a, uint32_t b,
+                                               OrderedAllocSmem<BLOCK>& sm, uint64_t& a_excl, uint64_t& b_excl,
+                                               uint64_t& total) {
+    uint64_t agg;
+    const uint64_t local = block_exclusive_scan<BLOCK>(((uint64_t)a << 31) | b, sm.warp, &agg);
+    const uint64_t base = lookback_prefix<BLOCK>(L, tile, agg, &sm.prefix);
+    a_excl = (base >> 31) + (local >> 31);
+    b_excl = (base & kLow31) + (local & kLow31);
+    total = base + agg;
+}
+
 }  // namespace fgc
