@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(kSetupTile) setup_kernel(GeomParams P) {
 
 // The FP64 half of setup: one thread per work item, every lane busy (the
 // work list holds only what survived culling), no barriers.
-__global__ void __launch_bounds__(256) setup_emit_kernel(GeomParams P) {
+__global__ void __launch_bounds__(256, 3) setup_emit_kernel(GeomParams P) {
     const uint64_t n = min((uint64_t)*P.work_total, P.work_cap);
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const SetupWork w = P.work[i];
