@@ -341,6 +341,9 @@ __global__ void __launch_bounds__(kSetupTile) setup_kernel(GeomParams P) {
 // The FP64 half of setup: one thread per work item, every lane busy (the
 // work list holds only what survived culling), no barriers.
 __global__ void __launch_bounds__(256, 3) setup_emit_kernel(GeomParams P) {
+    if (blockIdx.x == 0)  // each draw's primitive range: setup_kernel wrote the starts and the total
+        for (uint32_t i = threadIdx.x; i < P.nitems; i += blockDim.x)
+            P.iout[i].prim_end = (i + 1 < P.nitems) ? P.iout[i + 1].prim_start : *P.prim_total;
     const uint64_t n = min((uint64_t)*P.work_total, P.work_cap);
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const SetupWork w = P.work[i];
@@ -616,9 +619,4 @@ __global__ void __launch_bounds__(128) clip_lines_kernel(GeomParams P) {
 
 // Each draw's primitive range ends where the next draw's begins (the last
 // ends at the pass total). One thread per draw.
-__global__ void prim_ranges_kernel(GeomParams P) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.nitems; i += gridDim.x * blockDim.x)
-        P.iout[i].prim_end = (i + 1 < P.nitems) ? P.iout[i + 1].prim_start : *P.prim_total;
-}
-
 }  // namespace fgc

@@ -240,7 +240,6 @@ __global__ void setup_kernel(GeomParams P);
 __global__ void setup_emit_kernel(GeomParams P);
 __global__ void clip_triangles_kernel(GeomParams P);
 __global__ void clip_lines_kernel(GeomParams P);
-__global__ void prim_ranges_kernel(GeomParams P);
 
 __global__ void bin_count_kernel(BinParams P);
 __global__ void scan_u32_kernel(ScanParams P);

@@ -2,13 +2,14 @@
 // (any number of draws rendered with one launch per pipeline stage) and
 // reads their results back.
 //
-// A pass, all on one stream, no host wait inside:
+// A pass, no host wait inside:
 //   table upload              item views + lookup starts (pinned -> device)
 //   vertex_kernel             per draw, per unique position
 //   setup_kernel              draw by draw, triangles then lines, one ordered
-//                             allocation across the pass
+//                             allocation across the pass (slots and work items)
+//   setup_emit_kernel         the work items' raster primitives and each draw's
+//                             primitive range; beside it, on a second stream,
 //   clip_triangles / clip_lines_kernel
-//   prim_ranges_kernel        each draw's primitive range
 //   bin_count / scan_u32 / bin_scatter   per-draw band bins, one scan
 //   raster_kernel             persistent CTAs over the pass's (draw, band)
 //                             queue
@@ -493,10 +494,7 @@ int issue_submission(PassScratch& S, cudaStream_t stream, const DevLimits& D, co
         rec.launches++;
         if (clips) FGC_CUDA(cudaStreamWaitEvent(stream, S.ev_join, 0));
         mark(evs, stream);
-        prim_ranges_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, stream>>>(gp);
-        FGC_CUDA(cudaGetLastError());
-        rec.launches++;
-        mark(evs, stream);
+        mark(evs, stream);  // the stage the primitive ranges had (now part of the emission)
 
         BinParams bp;
         bp.items = items;
