@@ -262,6 +262,52 @@ __device__ void emit_triangle_piece(const GeomParams& P, const ItemView& I, uint
                     (uint32_t)t);
 }
 
+// One element's setup decision: its primitive slots (count), the
+// primitive-emitting pieces it hands to the emit kernel (work: a triangle,
+// each edge of a wireframe triangle, or a line), or a clip entry instead.
+struct SetupElem {
+    uint32_t count, work, u0, u1, u2;
+    int order;
+    bool clip;
+};
+__device__ __forceinline__ SetupElem classify(const GeomParams& P, const ItemView& I, bool tri, uint64_t k,
+                                              const uint8_t* vout) {
+    SetupElem e{0, 0, 0, 0, 0, 0, false};
+    if (tri) {
+        if (k >= I.tri_count) return e;
+        const int per = I.st.wireframe ? 6 : 1;
+        const uint64_t t = I.tri_first + k;
+        e.u0 = I.mesh.corner_uniq[3 * t + 0];
+        e.u1 = I.mesh.corner_uniq[3 * t + 1];
+        e.u2 = I.mesh.corner_uniq[3 * t + 2];
+        e.clip = (vout[e.u0] | vout[e.u1] | vout[e.u2]) != 0;
+        if (e.clip) {
+            // a triangle the clipper empties needs no clip entry or slots
+            const VClip* vc = P.vclip + I.vbase;
+            const VClip a = vc[e.u0], b = vc[e.u1], c = vc[e.u2];
+            if (!clip_leaves_something(d4(a.x, a.y, a.z, a.w), d4(b.x, b.y, b.z, b.w), d4(c.x, c.y, c.z, c.w)))
+                e.clip = false;  // order stays 0: no primitives
+        } else {
+            const double2* vndc = P.vndc + I.vbase;
+            const double2 n0 = vndc[e.u0], n1 = vndc[e.u1], n2 = vndc[e.u2];
+            e.order = cull_decision(I.st, n0.x, n0.y, n1.x, n1.y, n2.x, n2.y);
+        }
+        e.count = e.clip ? (uint32_t)(7 * per) : (e.order != 0 ? (uint32_t)per : 0u);
+        if (e.count != 0 && !e.clip) e.work = I.st.wireframe ? 3 : 1;
+    } else {
+        if (k >= I.line_count) return e;
+        e.count = 2;
+        const uint64_t cb = 3 * I.mesh.ntri + 2 * (I.line_first + k);
+        e.u0 = I.mesh.corner_uniq[cb];
+        e.u1 = I.mesh.corner_uniq[cb + 1];
+        e.clip = (vout[e.u0] | vout[e.u1]) != 0;
+        if (!e.clip) e.work = 1;
+    }
+    return e;
+}
+
+// kSetupPer consecutive elements per thread, so that the slots and work
+// items of a thread's elements follow one another.
 __global__ void __launch_bounds__(kSetupTile) setup_kernel(GeomParams P) {
     __shared__ uint32_t s_tile;
     __shared__ OrderedAllocSmem<kSetupTile> s_alloc;
@@ -270,71 +316,48 @@ __global__ void __launch_bounds__(kSetupTile) setup_kernel(GeomParams P) {
     const ItemView& I = P.items[item];
     const uint32_t lt = tile - I.stile0;
     const bool tri = lt < I.ntri_tiles;
-    const uint64_t k = (uint64_t)(tri ? lt : lt - I.ntri_tiles) * kSetupTile + threadIdx.x;
-    const bool valid = k < (tri ? I.tri_count : I.line_count);
+    const uint64_t k0 = (uint64_t)(tri ? lt : lt - I.ntri_tiles) * (kSetupTile * kSetupPer) +
+                        (uint64_t)kSetupPer * threadIdx.x;
     const uint8_t* vout = P.vout + I.vbase;
 
-    uint64_t count = 0;
-    uint32_t u0 = 0, u1 = 0, u2 = 0;
-    int order = 0;
-    bool clip = false;
-    // work: the primitive-emitting pieces this element hands to the emit
-    // kernel (a triangle, each edge of a wireframe triangle, or a line); an
-    // element that needs clipping instead takes a clip entry
-    uint32_t work = 0;
-    if (tri) {
-        const int per = I.st.wireframe ? 6 : 1;
-        if (valid) {
-            const uint64_t t = I.tri_first + k;
-            u0 = I.mesh.corner_uniq[3 * t + 0];
-            u1 = I.mesh.corner_uniq[3 * t + 1];
-            u2 = I.mesh.corner_uniq[3 * t + 2];
-            clip = (vout[u0] | vout[u1] | vout[u2]) != 0;
-            if (clip) {
-                // a triangle the clipper empties needs no clip entry or slots
-                const VClip* vc = P.vclip + I.vbase;
-                const VClip a = vc[u0], b = vc[u1], c = vc[u2];
-                if (!clip_leaves_something(d4(a.x, a.y, a.z, a.w), d4(b.x, b.y, b.z, b.w), d4(c.x, c.y, c.z, c.w)))
-                    clip = false;  // order stays 0: no primitives
-            } else {
-                const double2* vndc = P.vndc + I.vbase;
-                double2 n0 = vndc[u0], n1 = vndc[u1], n2 = vndc[u2];
-                order = cull_decision(I.st, n0.x, n0.y, n1.x, n1.y, n2.x, n2.y);
-            }
-            count = clip ? (uint64_t)(7 * per) : (order != 0 ? (uint64_t)per : 0);
-            if (count != 0 && !clip) work = I.st.wireframe ? 3 : 1;
-        }
-    } else if (valid) {
-        count = 2;
-        const uint64_t cb = 3 * I.mesh.ntri + 2 * (I.line_first + k);
-        u0 = I.mesh.corner_uniq[cb];
-        u1 = I.mesh.corner_uniq[cb + 1];
-        clip = (vout[u0] | vout[u1]) != 0;
-        if (!clip) work = 1;
+    SetupElem el[kSetupPer];
+    uint32_t count = 0, work = 0;
+#pragma unroll
+    for (int j = 0; j < kSetupPer; j++) {
+        el[j] = classify(P, I, tri, k0 + j, vout);
+        count += el[j].count;
+        work += el[j].work;
     }
     uint64_t slot, wpos, total;
-    ordered_alloc2<kSetupTile>(P.lb, tile, (uint32_t)count, work, s_alloc, slot, wpos, total);
+    ordered_alloc2<kSetupTile>(P.lb, tile, count, work, s_alloc, slot, wpos, total);
     if (lt == 0 && threadIdx.x == 0) P.iout[item].prim_start = slot;  // thread 0's local prefix is 0
     if (tile == gridDim.x - 1 && threadIdx.x == 0) {
         *P.prim_total = total >> 31;
         *P.work_total = total & kLow31;
     }
-    if (valid && count != 0 && clip) {
-        if (tri) {
-            append_clip(P, item, I.tri_first + k, slot);
-        } else {
-            uint32_t idx = atomicAdd(P.lclip_count, 1u);
-            P.lclip_list[idx] = ClipEntry{slot, (uint32_t)(I.line_first + k), item};  // holds every line of the pass
+#pragma unroll
+    for (int j = 0; j < kSetupPer; j++) {
+        const SetupElem& e = el[j];
+        const uint64_t k = k0 + j;
+        if (e.count != 0 && e.clip) {
+            if (tri) {
+                append_clip(P, item, I.tri_first + k, slot);
+            } else {
+                uint32_t idx = atomicAdd(P.lclip_count, 1u);
+                P.lclip_list[idx] = ClipEntry{slot, (uint32_t)(I.line_first + k), item};  // holds every line of the pass
+            }
         }
-    }
-    const uint32_t elem = (uint32_t)((tri ? I.tri_first : I.line_first) + k);
-    const uint32_t meta = (uint32_t)(order + 1) << 8 | (tri ? 0u : kWorkLine);
-    for (uint32_t w = 0; w < work; w++) {
-        if (wpos + w >= P.work_cap) {  // sized for every element: not reached
-            atomicOr(P.status, ST_RASTER_INTERNAL);
-            break;
+        const uint32_t elem = (uint32_t)((tri ? I.tri_first : I.line_first) + k);
+        const uint32_t meta = (uint32_t)(e.order + 1) << 8 | (tri ? 0u : kWorkLine);
+        for (uint32_t w = 0; w < e.work; w++) {
+            if (wpos + w >= P.work_cap) {  // sized for every element: not reached
+                atomicOr(P.status, ST_RASTER_INTERNAL);
+                break;
+            }
+            P.work[wpos + w] = SetupWork{slot, elem, item, e.u0, e.u1, e.u2, meta | w};
         }
-        P.work[wpos + w] = SetupWork{slot, elem, item, u0, u1, u2, meta | w};
+        slot += e.count;
+        wpos += e.work;
     }
 }
 

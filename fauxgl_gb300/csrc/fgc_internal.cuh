@@ -137,7 +137,8 @@ struct GeomParams {
     uint64_t work_cap;
     unsigned long long* work_total;
 };
-constexpr int kSetupTile = 256;
+constexpr int kSetupTile = 256;  // threads of a setup tile
+constexpr int kSetupPer = 2;     // consecutive elements per thread
 
 struct BinParams {
     const ItemView* items;

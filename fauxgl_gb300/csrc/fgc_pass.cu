@@ -169,8 +169,8 @@ int plan_pass(const Submission& sub, const std::vector<uint32_t>& idx, const Dev
                                               (uint64_t)2 * D.sms);
         const bool draws = it.tc > 0 || it.lc > 0;
         const uint32_t vt = draws ? (uint32_t)ceil_div(it.mesh->nuniq, kVertexTile) : 0;
-        v.ntri_tiles = (uint32_t)ceil_div(it.tc, kSetupTile);
-        v.nline_tiles = (uint32_t)ceil_div(it.lc, kSetupTile);
+        v.ntri_tiles = (uint32_t)ceil_div(it.tc, kSetupTile * kSetupPer);
+        v.nline_tiles = (uint32_t)ceil_div(it.lc, kSetupTile * kSetupPer);
         const uint32_t st = std::max<uint32_t>(1, v.ntri_tiles + v.nline_tiles);
         v.vtile0 = P.vtiles;
         v.stile0 = P.stiles;
