@@ -671,6 +671,164 @@ __device__ __forceinline__ uint32_t walk_row(uint32_t pp, const RPrim& R, const 
     return total;
 }
 
+// Applies one queued covered pixel of a warp: barycentrics b = w*ra and the
+// depth with the owning lane's ra and vertex depths (fetched by shuffle:
+// every lane of the warp calls this), then early depth rejection and the
+// fragment record, as walk_row does for its own pixels.
+__device__ __forceinline__ void flush_queued(uint32_t n, uint32_t q0, double ra, double z0, double z1, double z2,
+                                             const RasterParams& P, const ItemView& I, const BandCtx& B,
+                                             RasterSmem& S, uint32_t* s_nfrag, uint32_t* s_conflict) {
+    const uint32_t lane = threadIdx.x & 31, e = q0 + lane;
+    const int src = lane < n ? (int)S.ucnt[e] : (int)lane;
+    const double rai = __shfl_sync(0xffffffffu, ra, src);
+    const double z0i = __shfl_sync(0xffffffffu, z0, src);
+    const double z1i = __shfl_sync(0xffffffffu, z1, src);
+    const double z2i = __shfl_sync(0xffffffffu, z2, src);
+    if (lane >= n) return;
+    const uint32_t key = (uint32_t)S.ux[e];
+    const uint32_t pix = key >> 16;
+    const double b0 = __dmul_rn(S.uw0[e], rai);
+    const double b1 = __dmul_rn(S.uw1[e], rai);
+    const double b2 = __dmul_rn(S.uw2[e], rai);
+    const double z = __dadd_rn(__dadd_rn(__dmul_rn(b0, z0i), __dmul_rn(b1, z1i)), __dmul_rn(b2, z2i));
+    const double bias = I.st.depth_bias;
+    if (B.early && dgt_i(add_bias(z, bias, dbits(bias) == 0), S.depth[pix])) return;
+    const uint32_t slot = atomicAdd(s_nfrag, 1u);
+    if (slot >= (uint32_t)P.F) {
+        atomicOr(s_conflict, 2u);
+        return;
+    }
+    S.fb0[slot] = b0;
+    S.fb1[slot] = b1;
+    S.fb2[slot] = b2;
+    S.fz[slot] = z;
+    S.fkey[slot] = key;
+    unsigned short* hd = &S.head[bucket_of(pix)];
+    unsigned short old = *hd, assumed;
+    do {
+        assumed = old;
+        old = atomicCAS(hd, assumed, (unsigned short)slot);
+    } while (old != assumed);
+    S.nxt[slot] = old;
+    if (old != 0xFFFFu) atomicOr(s_conflict, 1u);
+}
+
+// walk_row for a direct chunk with one unit per thread, every thread of the
+// block taking part (has: the thread holds a unit). The row loops run in
+// step across the warp; a covered in-band pixel is queued (edge values, band
+// pixel, unit, owning lane) in the warp's 32 entries of the span arrays,
+// which direct chunks do not use, and each full queue is applied with all
+// 32 lanes busy, so the pixel's 8 FP64 operations cost one warp instruction
+// per 32 pixels rather than one per step in which any lane is covered. A
+// direct chunk's boxes are at most kNarrow wide, which bounds the loop.
+__device__ __forceinline__ uint32_t walk_rows_queued(bool has, uint32_t pp, const RPrim& R, const PBox& bx,
+                                                     int32_t y, const RasterParams& P, const ItemView& I,
+                                                     const BandCtx& B, RasterSmem& S, uint32_t unit,
+                                                     uint32_t* s_nfrag, uint32_t* s_conflict, uint64_t& visited) {
+    const uint32_t lane = threadIdx.x & 31, q0 = threadIdx.x & ~31u;  // this warp's queue entries
+    double w0 = 0, w1 = 0, w2 = 0, a0 = 0, a1 = 0, a2 = 0, ra = 0, z0 = 0, z1 = 0, z2 = 0;
+    RaSign rs{0, false};
+    bool active = false, was = false, s0 = false, s1 = false, s2 = false;
+    int32_t x = 0, x1 = 0, rel = 0;
+    if (has) {
+        double w00, w01, w02;
+        row_start(P, pp, R, bx, y, I, B, w00, w01, w02);
+        double d = 0;
+        const double d0 = __dmul_rn(-w00, R.q0);
+        const double d1 = __dmul_rn(-w01, R.q1);
+        const double d2 = __dmul_rn(-w02, R.q2);
+        if (dlt0(w00) && dgt_i(d0, d)) d = d0;
+        if (dlt0(w01) && dgt_i(d1, d)) d = d1;
+        if (dlt0(w02) && dgt_i(d2, d)) d = d2;
+        int64_t di = go_f2i_i(d);  // d = float64(int(d)); if d < 0 { d = 0 }
+        if (di < 0) di = 0;
+        if (di <= (int64_t)bx.x1 - bx.x0) {  // else the row loop starts past x1
+            d = i2d_i(di);
+            a0 = R.a0;
+            a1 = R.a1;
+            a2 = R.a2;
+            w0 = __dadd_rn(w00, __dmul_rn(a0, d));
+            w1 = __dadd_rn(w01, __dmul_rn(a1, d));
+            w2 = __dadd_rn(w02, __dmul_rn(a2, d));
+            ra = R.ra;
+            rs = ra_sign(ra);
+            s0 = stays_out(a0, ra);
+            s1 = stays_out(a1, ra);
+            s2 = stays_out(a2, ra);
+            z0 = R.z0;
+            z1 = R.z1;
+            z2 = R.z2;
+            x = bx.x0 + (int32_t)di;
+            x1 = bx.x1;
+            rel = (y - B.r0) * I.W;
+            active = true;
+        }
+    }
+    uint32_t total = 0, qn = 0;
+    while (__any_sync(0xffffffffu, active)) {
+        bool cov = false;
+        double c0 = 0, c1 = 0, c2 = 0;
+        int32_t pix = 0;
+        if (active) {
+            c0 = w0;
+            c1 = w1;
+            c2 = w2;
+            w0 = __dadd_rn(c0, a0);
+            w1 = __dadd_rn(c1, a1);
+            w2 = __dadd_rn(c2, a2);
+            visited++;
+            const bool o0 = neg_product(c0, ra, rs), o1 = neg_product(c1, ra, rs), o2 = neg_product(c2, ra, rs);
+            if (o0 || o1 || o2) {
+                // rasterize breaks after the covered run; before it, an edge
+                // the row can only leave ends the row as well
+                if (was || (o0 && s0) || (o1 && s1) || (o2 && s2)) active = false;
+            } else {
+                was = true;
+                // i = y*W + x is skipped outside [0, W*H) (context.go:223-228);
+                // here only this band's part of that range is drawn
+                pix = rel + x;
+                if (pix >= B.npx) {
+                    active = false;  // no later pixel of the row is in the band
+                } else if (pix >= 0) {
+                    total++;
+                    cov = true;
+                }
+            }
+            if (active && ++x > x1) active = false;
+        }
+        const uint32_t cm = __ballot_sync(0xffffffffu, cov);
+        if (cm == 0) continue;
+        const uint32_t pos = qn + (uint32_t)__popc(cm & ((1u << lane) - 1u));
+        const uint32_t key = ((uint32_t)pix << 16) | unit;
+        if (cov && pos < 32) {
+            S.uw0[q0 + pos] = c0;
+            S.uw1[q0 + pos] = c1;
+            S.uw2[q0 + pos] = c2;
+            S.ux[q0 + pos] = (int32_t)key;
+            S.ucnt[q0 + pos] = lane;
+        }
+        qn += (uint32_t)__popc(cm);
+        if (qn >= 32) {
+            __syncwarp();
+            flush_queued(32, q0, ra, z0, z1, z2, P, I, B, S, s_nfrag, s_conflict);
+            __syncwarp();
+            if (cov && pos >= 32) {
+                S.uw0[q0 + pos - 32] = c0;
+                S.uw1[q0 + pos - 32] = c1;
+                S.uw2[q0 + pos - 32] = c2;
+                S.ux[q0 + pos - 32] = (int32_t)key;
+                S.ucnt[q0 + pos - 32] = lane;
+            }
+            qn -= 32;
+        }
+    }
+    if (qn) {
+        __syncwarp();
+        flush_queued(qn, q0, ra, z0, z1, z2, P, I, B, S, s_nfrag, s_conflict);
+    }
+    return total;
+}
+
 // Fragments of one piece of a row: len covered in-band pixels from band pixel pix,
 // edge values w at the first. Early depth rejection, fragment records, and
 // the push onto the pixel bucket lists (a non-empty list is a possible
@@ -1116,10 +1274,20 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
                 }
                 __syncthreads();
                 uint64_t tchunk = 0;
-                for (uint32_t u = threadIdx.x; u < nunit; u += blockDim.x) {
-                    const uint32_t pp = S.cprim[S.uslot[u]];
-                    tchunk += walk_row(pp, P.prims[pp], P.pbox[pp], S.urow[u], P, I, B, S, u, &s_nfrag, &s_conflict,
-                                       vis);
+                if (P.su >= kRT) {
+                    // the span arrays hold a 32-entry queue per warp: every
+                    // thread takes part, a unit each (nunit <= kRT here)
+                    const uint32_t u = threadIdx.x;
+                    const bool has = u < nunit;
+                    const uint32_t pp = has ? S.cprim[S.uslot[u]] : 0u;
+                    tchunk += walk_rows_queued(has, pp, P.prims[pp], P.pbox[pp], has ? S.urow[u] : 0, P, I, B, S, u,
+                                               &s_nfrag, &s_conflict, vis);
+                } else {
+                    for (uint32_t u = threadIdx.x; u < nunit; u += blockDim.x) {
+                        const uint32_t pp = S.cprim[S.uslot[u]];
+                        tchunk += walk_row(pp, P.prims[pp], P.pbox[pp], S.urow[u], P, I, B, S, u, &s_nfrag,
+                                           &s_conflict, vis);
+                    }
                 }
                 {
                     // the next chunk's entries load during this one's shading
