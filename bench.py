@@ -75,9 +75,11 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per rate of the serving loop")
     ap.add_argument("--serve-max-requests", type=int, default=160, help="requests per rate at most")
     ap.add_argument("--serve-budget-gb", type=int, default=96, help="HBM budget of the serving loop")
-    ap.add_argument("--only", choices=["all", "plain", "mixed", "ss16", "batch", "serve", "meshprep"], default="all",
-                    help="plain / mixed / ss16 / batch / serve: time only the plain or mixed 1080p frame, the plain "
-                         "16x supersampled frame, the thumbnail batch or the serving loop (for profiler runs)")
+    ap.add_argument("--only", choices=["all", "plain", "mixed", "ss16", "batch", "serve", "meshprep", "accuracy"],
+                    default="all",
+                    help="plain / mixed / ss16 / batch / serve / meshprep: time only that workload (for profiler "
+                         "runs); accuracy: only the per-configuration comparison with the oracle")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the comparison with the oracle")
     return ap.parse_args()
 
 
@@ -580,13 +582,113 @@ def bench_serve(args, meshes):
     return out
 
 
+ACCURACY_NOTE = ("checker leg, outside every timed region: each configuration drawn once per form through the C ABI "
+                 "and compared with the oracle (the FP64 C restatement in the reference's sequential order) on the "
+                 "same inputs; colour errors per NRGBA channel as fractions of full scale (1/255 = 0.00392), "
+                 "shaded_* the pre-quantisation shader output where the winners agree")
+
+
+def _accuracy_frame(lib, mesh_h, w, h, draws, precision, ref, shaded, clear):
+    """One GPU frame of the draws with winner (and shaded-colour) debug
+    outputs, compared with the oracle frame ref."""
+    from fauxgl_gb300 import _abi
+    from fauxgl_gb300.context import NewContext
+    from oracle import oracle as O
+    ctx = NewContext(w, h)
+    ctx.SetDebug(_abi.FGC_DEBUG_WINNER | (_abi.FGC_DEBUG_SHADED_COLOR if shaded else 0))
+    ctx.ClearColorBufferWith(clear)
+    for st, sh in draws:
+        st = _abi.FgcState.from_buffer_copy(st)
+        st.precision = precision
+        info = _abi.FgcRasterizeInfo()
+        _abi.check(lib.fgc_draw_mesh(ctx.handle, mesh_h, ctypes.byref(st), ctypes.byref(sh), ctypes.byref(info)))
+    err = O.frame_error(ctx.Image(), ctx.DepthBuffer, ctx.Winner(), ref, shaded=ctx.ShadedColor() if shaded else None)
+    return ctx, err
+
+
+def bench_accuracy(lib, dense, dense_h):
+    """Max and mean per-channel colour error and the winner-mismatch fraction
+    of both forms against the FP64 oracle, for the 512^2 icosphere frame, the
+    dense 1080p frame, the 16x supersampled frame with its overlay (and its
+    downsampled image) and a covering subset of the thumbnail views."""
+    import numpy as np
+    from fauxgl_gb300 import _abi, scenes
+    from fauxgl_gb300.context import _upload_mesh
+    from fauxgl_gb300.shader import NewPhongShader, to_fgc_shader
+    from oracle import oracle as O
+    forms = (("plain", _abi.FGC_PRECISION_PLAIN), ("mixed", _abi.FGC_PRECISION_MIXED))
+    out = {"note": ACCURACY_NOTE}
+    t0 = time.time()
+
+    def one(name, mesh, mesh_h, w, h, draws, shaded=True, scale=1):
+        ref = O.OracleContext(w, h)
+        ref.clear_color(scenes.BACKGROUND)
+        for st, sh in draws:
+            ref.draw(mesh, st, sh)
+        res = {}
+        for form, prec in forms:
+            ctx, err = _accuracy_frame(lib, mesh_h, w, h, draws, prec, ref, shaded, scenes.BACKGROUND)
+            if scale > 1:
+                d = np.abs(ctx.Downsample(scale).astype(np.int16) - O.downsample(ref.color(), scale).astype(np.int16))
+                err["downsampled"] = {"max_err": round(float(d.max()) / 255.0, 6),
+                                      "mean_err": float("%.3g" % (float(d.mean()) / 255.0))}
+            res[form] = err
+        out[name] = res
+
+    st0 = _abi.state_default()
+    c0 = scenes.sphere_scene(4)
+    one("c0_sphere_512", c0, _upload_mesh(c0), 512, 512, [(st0, phong_struct(512, 512))])
+    one("c1_dense_1080p", dense, dense_h, W, H, [(st0, phong_struct(W, H))])
+    st2 = _abi.state_default()
+    st2.wireframe, st2.depth_bias = 1, 1e-5
+    one("c2_dense_16xss_overlay", dense, dense_h, W * SS, H * SS,
+        [(st0, phong_struct(W * SS, H * SS)), (st2, overlay_struct(W * SS, H * SS))], shaded=False, scale=SS)
+    # a covering subset of the thumbnail batch, each view compared on its own
+    _, views = scenes.thumbnail_batch(build=set())
+    pick = scenes.thumbnail_check_views(views)
+    meshes, views = scenes.thumbnail_batch(build={views[i]["mesh"] for i in pick})
+    agg = {form: {"pixels": 0, "max_err": 0.0, "sum_err": 0.0, "winner_mismatches": 0, "depth_mismatches": 0,
+                  "shaded_max_err": 0.0} for form, _ in forms}
+    for i in pick:
+        v = views[i]
+        m = meshes[v["mesh"]]
+        sh = NewPhongShader(v["matrix"], scenes.LIGHT, v["eye"])
+        sh.ObjectColor = v["color"]
+        shs = to_fgc_shader(sh)
+        ref = O.OracleContext(v["width"], v["height"])
+        ref.clear_color(scenes.BACKGROUND)
+        ref.draw(m, st0, shs)
+        for form, prec in forms:
+            _, err = _accuracy_frame(lib, _upload_mesh(m), v["width"], v["height"], [(st0, shs)], prec, ref, True,
+                                     scenes.BACKGROUND)
+            a = agg[form]
+            n = err["pixels"]
+            a["pixels"] += n
+            a["max_err"] = max(a["max_err"], err["max_err"])
+            a["sum_err"] += err["mean_err"] * n
+            a["winner_mismatches"] += round(err["winner_mismatch_frac"] * n)
+            a["depth_mismatches"] += round(err["depth_mismatch_frac"] * n)
+            a["shaded_max_err"] = max(a["shaded_max_err"], err["shaded_max_err"])
+    out["c3_thumbnail_views"] = {"views": len(pick), "kinds_x_resolutions": len({(views[i]["kind"], views[i]["width"])
+                                                                                  for i in pick})}
+    for form, _ in forms:
+        a = agg[form]
+        out["c3_thumbnail_views"][form] = {
+            "pixels": a["pixels"], "max_err": a["max_err"],
+            "mean_err": float("%.3g" % (a["sum_err"] / max(a["pixels"], 1))),
+            "winner_mismatch_frac": a["winner_mismatches"] / max(a["pixels"], 1),
+            "depth_mismatch_frac": a["depth_mismatches"] / max(a["pixels"], 1),
+            "shaded_max_err": a["shaded_max_err"]}
+    out["seconds"] = round(time.time() - t0, 1)
+    return out
+
+
 def cpu_frames(mesh, nframes, nthreads):
     """The oracle's threaded form (the reference's own worker split) on the
     host cores: one warm-up frame, then the median of nframes."""
     from fauxgl_gb300 import _abi, scenes
     from oracle import oracle as O
-    st = _abi.FgcState()
-    _abi.load_library().fgc_state_default(ctypes.byref(st))
+    st = _abi.state_default()
     sh = phong_struct(W, H)
     ctx = O.OracleContext(W, H)
     times = []
@@ -601,19 +703,38 @@ def cpu_frames(mesh, nframes, nthreads):
     return statistics.median(times), times
 
 
-def profile_traffic():
-    """DRAM bytes per launch of the raster kernel from the committed ncu
-    summary (a 'traffic_bytes_per_launch: N' line), or None."""
-    p = os.path.join(ROOT, "profiles", "raster_kernel_dense1080p.md")
+# Algorithmic HBM bytes of a frame (each byte the frame must move once): the
+# mesh's per-corner records the plain form reads (position + normal, 2 x 3
+# FP64 per corner, 144 B per triangle) and one fused clear-and-write pass of
+# the NRGBA colour (4 B) and FP64 depth (8 B) of every pixel.
+BYTES_PER_TRIANGLE_PLAIN = 144
+BYTES_PER_PIXEL = 12
+
+
+def load_profile(name):
+    """A committed ncu summary (profiles/<name>.json): the DRAM traffic per
+    launch of a kernel of this version, with the command that measured it."""
+    p = os.path.join(ROOT, "profiles", name + ".json")
     if not os.path.exists(p):
         return None
-    for line in open(p):
-        if line.strip().startswith("traffic_bytes_per_launch:"):
-            try:
-                return int(line.split(":", 1)[1].strip().split()[0])
-            except ValueError:
-                return None
-    return None
+    with open(p) as f:
+        return json.load(f)
+
+
+def hbm_peak():
+    """(GB/s, source): the measured copy bandwidth of the GB300s
+    (MEASURED_PEAKS.json hbm_gbs) when the file is present, else the value it
+    held when it was last present here."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        for k in ("hbm_gbs", "hbm_GBps", "hbm"):
+            if isinstance(d.get(k), (int, float)):
+                return float(d[k]), "measured (MEASURED_PEAKS.json %s)" % k
+    except (OSError, ValueError, AttributeError):
+        pass
+    return 6694.5, "measured copy bandwidth of this pool's GB300s (MEASURED_PEAKS.json hbm_gbs, as last recorded)"
 
 
 def run_reference(args):
@@ -624,8 +745,7 @@ def run_reference(args):
     mesh = build_scene()
     from fauxgl_gb300 import _abi, scenes
     from oracle import oracle as O
-    st = _abi.FgcState()
-    _abi.load_library().fgc_state_default(ctypes.byref(st))
+    st = _abi.state_default()
     sh = phong_struct(W, H)
     ctx = O.OracleContext(W, H)
 
@@ -713,6 +833,9 @@ def main():
     if args.only == "meshprep":
         print(json.dumps({"meshprep": bench_meshprep(lib, mesh, torch)}), flush=True)
         return 0
+    if args.only == "accuracy":
+        print(json.dumps({"accuracy": bench_accuracy(lib, mesh, mesh_h)}), flush=True)
+        return 0
 
     # ---- headline: plain FP64 at 1080p, mesh resident ------------------------
     # nvidia-smi samples the clocks over all GPU measurements below.
@@ -783,6 +906,10 @@ def main():
     if args.only == "all" and pool is not None:
         serve = bench_serve(args, pool)
     clocks.__exit__(None, None, None)
+    accuracy = None
+    if args.only == "all" and not args.no_accuracy and rank == 0 and world == 1:
+        accuracy = bench_accuracy(lib, mesh, mesh_h)
+        log("accuracy:", json.dumps(accuracy))
 
     # ---- roofline of the dominant stage --------------------------------------
     names = list(_abi.STAGE_NAMES)
@@ -797,10 +924,13 @@ def main():
     else:
         flops = 0
     achieved = flops / (stage[dom] * 1e-3) / 1e12 if stage[dom] > 0 else 0.0
-    # HBM view of the raster stage: framebuffer store (fused clear) + bins +
-    # primitive records + per-fragment vertex attributes
-    raster_bytes = (W * H * 12 + st.bin_entries * (4 + 176 + 16) + st.shaded_fragments * 3 * 48)
-    traffic = profile_traffic()
+    # HBM view of the frame: algorithmic bytes (mesh records once, one
+    # framebuffer pass) over the whole frame's time, and the raster kernel's
+    # measured DRAM traffic per launch from the committed ncu summary
+    frame_bytes = st.elements * BYTES_PER_TRIANGLE_PLAIN + W * H * BYTES_PER_PIXEL
+    gbs_peak, gbs_src = hbm_peak()
+    prof = load_profile("raster_kernel_dense1080p")
+    traffic = prof.get("plain", {}).get("dram_bytes_per_launch") if prof else None
 
     # ---- CPU baseline (rank 0, N=1 only) ------------------------------------
     cpu = None
@@ -832,10 +962,18 @@ def main():
             "roofline": {"bound": "fp64", "kernel": names[dom] + "_kernel", "achieved": round(achieved, 4),
                          "peak": round(fp64_peak_tflops, 4), "unit": "TFLOP/s",
                          "frac": round(achieved / fp64_peak_tflops, 4) if fp64_peak_tflops else None,
-                         "traffic": traffic, "peak_source": "measured FP64 add rate (fgc_measure_fp64_rate)",
-                         "hbm": {"achieved": round(raster_bytes / (stage[4] * 1e-3) / 1e9, 1) if stage[4] else None,
-                                 "peak": 6694.5, "unit": "GB/s", "kernel": "raster_kernel",
-                                 "peak_source": "MEASURED_PEAKS.json hbm_gbs"}},
+                         "traffic": traffic,
+                         "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
+                                            "profiles/raster_kernel_dense1080p.json (%s)" % prof.get("version", "?"))
+                         if prof else None,
+                         "peak_source": "FP64 add rate measured in this run by the library's own probe "
+                                        "(fgc_measure_fp64_rate; the pool's MEASURED_PEAKS.json has no FP64 figure)",
+                         "flops_per_launch": int(flops),
+                         "hbm": {"bound_of": "whole frame", "algorithmic_bytes": int(frame_bytes),
+                                 "achieved": round(frame_bytes / (ms * 1e-3) / 1e9, 1),
+                                 "peak": gbs_peak, "unit": "GB/s",
+                                 "frac": round(frame_bytes / (ms * 1e-3) / 1e9 / gbs_peak, 4),
+                                 "peak_source": gbs_src}},
             "stages_ms": {n: round(v, 4) for n, v in zip(names, stage)},
             "work": {"elements": st.elements, "unique_vertices": st.unique_vertices, "clipped": st.clipped,
                      "primitives": st.primitives, "bin_entries": st.bin_entries,
@@ -847,6 +985,7 @@ def main():
             "batch": batch,
             "serve": serve,
             "meshprep": meshprep,
+            "accuracy": accuracy,
             "clocks": clocks.summary(),
         }
         if cpu is not None:

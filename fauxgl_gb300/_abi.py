@@ -52,6 +52,14 @@ class FgcState(ctypes.Structure):
     ]
 
 
+def state_default():
+    """An fgc_state holding NewContext's defaults (context.go:66-77): ReadDepth,
+    WriteDepth, WriteColor and AlphaBlend on, Wireframe off, FaceCCW, CullBack,
+    LineWidth 2, DepthBias 0, plain precision. The same values as the
+    library's fgc_state_default, built without loading the library."""
+    return FgcState(1, 1, 1, 1, 0, FGC_FACE_CCW, FGC_CULL_BACK, FGC_PRECISION_PLAIN, 2.0, 0.0)
+
+
 class FgcShader(ctypes.Structure):
     _fields_ = [
         ("kind", ctypes.c_int32),

@@ -306,6 +306,10 @@ void fgc_shader_phong(fgc_shader* sh, const double matrix[16], const double ligh
     sh->specular_power = 32;
 }
 
+namespace {
+int noalloc_prepare(int device);
+}
+
 int fgc_context_create(int32_t width, int32_t height, fgc_context** out) {
     if (!out) return fail(FGC_ERR_INVALID_ARGUMENT, "out is null");
     *out = nullptr;
@@ -335,6 +339,10 @@ int fgc_context_create(int32_t width, int32_t height, fgc_context** out) {
     c->clear_color_pending = true;
     c->clear_depth = 1.7976931348623157e308;
     c->clear_depth_pending = true;
+    // fgc_depth_image_noalloc's static scratch and kernels are made resident
+    // here, so that the entry point itself never makes the driver allocate
+    int rc = noalloc_prepare(c->device);
+    if (rc) return bail(rc);
     *out = c;
     return FGC_OK;
 }
@@ -707,15 +715,18 @@ int fgc_read_shaded_color(fgc_context* c, double* rgba) {
 // admits work, a host application that owns the GPU memory of its plugins)
 // use fgc_depth_image_noalloc instead: the same two kernels, with the
 // min/max pair and the Gray16 staging image placed in the static array
-// below. The array is reserved on every GPU that loads the library until the
-// process exits, which is why it is kept to 16 MiB: frames up to
-// FGC_DEPTH_IMAGE_NOALLOC_MAX_PIXELS (2^23) pixels.
+// below. The array is reserved on a GPU when the first context on it is
+// created and stays until the process exits, which is why it is kept to
+// 16 MiB: frames up to FGC_DEPTH_IMAGE_NOALLOC_MAX_PIXELS (2^23) pixels.
 //
-// Host code cannot use the array's name as a device address; the first call
-// on each device, with that device current, looks the address up with
-// cudaGetSymbolAddress and keeps it (so that first call should come before
-// any stream capture). Every call re-initialises the min/max pair it needs,
-// and every call uses the same array, so calls that overlap on the GPU race.
+// Host code cannot use the array's name as a device address. When the first
+// context on a device is created (fgc_context_create, with that device
+// current) the address is looked up with cudaGetSymbolAddress and kept, and
+// the two kernels are loaded: with CUDA's lazy module loading both steps
+// make the driver reserve device memory, so they happen at start-up and not
+// inside the entry point. Every call re-initialises the min/max pair it
+// needs, and every call uses the same array, so calls that overlap on the GPU
+// race.
 // ===========================================================================
 namespace {
 
@@ -727,17 +738,33 @@ static __device__ __align__(256) unsigned char g_depth_image_scratch[kNoAllocByt
 std::mutex g_noalloc_mu;
 void* g_noalloc_ptr[256] = {};
 
+// Once per device, with the device current: the scratch address and the
+// kernels the entry point launches (cudaFuncGetAttributes loads a lazily
+// loaded kernel).
+int noalloc_prepare(int device) {
+    if (device < 0 || device >= 256) return fail(FGC_ERR_UNSUPPORTED, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (g_noalloc_ptr[device]) return FGC_OK;
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_depth_image_scratch);
+    if (e != cudaSuccess || !p)
+        return fail(FGC_ERR_CUDA, std::string("cudaGetSymbolAddress(depth image scratch): ") + cudaGetErrorString(e));
+    cudaFuncAttributes fa;
+    e = cudaFuncGetAttributes(&fa, depth_minmax_kernel);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, depth_image_kernel);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, fill_u32_kernel);  // pending clears
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, fill_f64_kernel);
+    if (e != cudaSuccess)
+        return fail(FGC_ERR_CUDA, std::string("loading the depth image kernels: ") + cudaGetErrorString(e));
+    g_noalloc_ptr[device] = p;
+    return FGC_OK;
+}
+
+// The scratch of a device prepared by fgc_context_create.
 int noalloc_scratch(int device, unsigned char** out) {
     if (device < 0 || device >= 256) return fail(FGC_ERR_UNSUPPORTED, "device ordinal out of range");
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[device]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_depth_image_scratch);
-        if (e != cudaSuccess || !p)
-            return fail(FGC_ERR_CUDA, std::string("cudaGetSymbolAddress(depth image scratch): ") +
-                                          cudaGetErrorString(e));
-        g_noalloc_ptr[device] = p;
-    }
+    if (!g_noalloc_ptr[device]) return fail(FGC_ERR_INVALID_ARGUMENT, "no context was created on this device");
     *out = (unsigned char*)g_noalloc_ptr[device];
     return FGC_OK;
 }

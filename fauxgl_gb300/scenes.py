@@ -111,7 +111,7 @@ def phong_params(matrix, light=LIGHT, eye=EYE, color=OBJECT_COLOR):
 
 
 def thumbnail_batch(nmeshes=256, views_per_mesh=4, seed=3, tri_min=200, tri_max=200000,
-                    resolutions=(256, 512, 768, 1024)):
+                    resolutions=(256, 512, 768, 1024), build=None):
     """Batched-thumbnail workload: nmeshes seeded meshes whose triangle counts
     are log-uniform in [tri_min, tri_max] (displaced icospheres at the nearest
     subdivision level, cylinders and cones with 8-512 segments), each seen by
@@ -120,14 +120,25 @@ def thumbnail_batch(nmeshes=256, views_per_mesh=4, seed=3, tri_min=200, tri_max=
     random Phong object colour.
 
     Returns (meshes, views) where views is a list of dicts with keys
-    mesh, width, height, matrix, eye, color."""
+    mesh, kind ("sphere", "cylinder" or "cone"), segments (0 for spheres),
+    triangles, width, height, matrix, eye, color. build: a set of mesh indices to build
+    (the others are None; the draws of the seeded generator are the same)."""
     rng = SplitMix64(seed)
-    meshes = []
+    meshes, kinds = [], []
     for i in range(nmeshes):
         t = math.exp(math.log(tri_min) + rng.uniform() * (math.log(tri_max) - math.log(tri_min)))
         kind = int(rng.uniform() * 3)
-        if kind == 0:
+        seg = detail = 0
+        if kind != 0:
+            seg = int(math.exp(math.log(8) + rng.uniform() * (math.log(512) - math.log(8))))
+            ntri = seg * (4 if kind == 1 else 2)
+        else:
             detail = int(min(6, max(2, round(math.log(t / 20.0, 4)))))
+            ntri = 20 * 4 ** detail
+        kinds.append((("sphere", "cylinder", "cone")[kind], seg, ntri))
+        if build is not None and i not in build:
+            meshes.append(None)
+        elif kind == 0:
             pos = displace(sphere_positions(detail), seed * 1000003 + i)
             m = Mesh(pos)
             m.BiUnitCube()
@@ -135,10 +146,10 @@ def thumbnail_batch(nmeshes=256, views_per_mesh=4, seed=3, tri_min=200, tri_max=
             m.tri_nrm = np.ascontiguousarray(np.repeat(fn[:, None, :], 3, axis=1))
             smooth_normals_threshold_host(m, Radians(30.0))
         else:
-            seg = int(math.exp(math.log(8) + rng.uniform() * (math.log(512) - math.log(8))))
             m = cylinder_segments(seg, capped=True, cone=(kind == 2))
             m.BiUnitCube()
-        meshes.append(m)
+        if build is None or i in build:
+            meshes.append(m)
     views = []
     for i in range(nmeshes):
         for _ in range(views_per_mesh):
@@ -147,6 +158,30 @@ def thumbnail_batch(nmeshes=256, views_per_mesh=4, seed=3, tri_min=200, tri_max=
             eye = Vector(3 * math.cos(el) * math.cos(az), 3 * math.sin(el), 3 * math.cos(el) * math.sin(az))
             res = resolutions[int(rng.uniform() * len(resolutions))]
             color = (rng.uniform(), rng.uniform(), rng.uniform(), 1.0)
-            views.append(dict(mesh=i, width=res, height=res, eye=eye,
+            views.append(dict(mesh=i, kind=kinds[i][0], segments=kinds[i][1], triangles=kinds[i][2], width=res, height=res, eye=eye,
                               matrix=camera_matrix(res, res, eye=eye, center=V(0, 0, 0)), color=color))
     return meshes, views
+
+
+def thumbnail_check_views(views, count=16):
+    """A seeded subset of the thumbnail batch that covers it: the first view
+    of every (shape kind, resolution) pair, then views of the cylinders and
+    cones with the fewest and the most segments and of the largest meshes,
+    until count views are taken. Returns view indices in batch order."""
+    picked, seen = [], set()
+    for i, v in enumerate(views):
+        key = (v["kind"], v["width"])
+        if key not in seen:
+            seen.add(key)
+            picked.append(i)
+    lathe = [i for i, v in enumerate(views) if v["kind"] != "sphere"]
+    cands = []
+    if lathe:
+        cands += [min(lathe, key=lambda i: views[i]["segments"]), max(lathe, key=lambda i: views[i]["segments"])]
+    cands += sorted(range(len(views)), key=lambda i: (-views[i]["triangles"], -views[i]["width"], i))
+    for i in cands:
+        if len(picked) >= count:
+            break
+        if i not in picked:
+            picked.append(i)
+    return sorted(picked)

@@ -2,9 +2,8 @@
  * fauxglcuda.h -- C ABI of libfauxglcuda, the GB300 (sm_103a) implementation of
  * FauxGL's triangle pipeline.
  *
- * The ABI is what a cgo wrapper of package fauxgl binds:
- * plain C types, opaque handles, host arrays borrowed only for the duration of
- * a call. Every function returns an fgc_status (0 = FGC_OK). A failing call
+ * The ABI is what a cgo wrapper of package fauxgl binds: plain C types,
+ * opaque handles, host arrays borrowed only for the duration of a call. Every function returns an fgc_status (0 = FGC_OK). A failing call
  * leaves a message retrievable with fgc_last_error().
  *
  * Reference interfaces replaced (file:line in fogleman/fauxgl):
@@ -233,11 +232,11 @@ int fgc_depth_image(fgc_context* ctx, uint16_t* gray16);
  * after start-up -- a render service that sizes every buffer before it admits
  * requests, or a host application that owns the device memory of the plugins
  * it loads -- calls this instead. The scratch is one static 16 MiB device
- * array, reserved on every GPU that loads the library until the process
- * exits, so frames are limited to FGC_DEPTH_IMAGE_NOALLOC_MAX_PIXELS pixels;
- * larger contexts get FGC_ERR_INVALID_ARGUMENT. The first call on a device
- * looks the array up on that device (make it before any stream capture).
- * All calls share the array: calls that overlap on the GPU race. */
+ * array, reserved on a GPU (together with the kernels this call launches)
+ * when the first context on that GPU is created, and held until the process
+ * exits; frames are limited to FGC_DEPTH_IMAGE_NOALLOC_MAX_PIXELS pixels and
+ * larger contexts get FGC_ERR_INVALID_ARGUMENT. All calls share the array:
+ * calls that overlap on the GPU race. */
 #define FGC_DEPTH_IMAGE_NOALLOC_MAX_PIXELS 8388608
 int fgc_depth_image_noalloc(fgc_context* ctx, uint16_t* gray16);
 /* Box-downsample the colour buffer by an integer factor on the device:

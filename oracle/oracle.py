@@ -153,6 +153,44 @@ class OracleContext:
         return out.reshape(self.height, self.width)
 
 
+def frame_error(image, depth, winner, ref, shaded=None):
+    """Accuracy of a rendered frame against the oracle's frame `ref` (an
+    OracleContext drawn with the same calls): the checker behind the parity
+    tests and the benchmark's accuracy report.
+
+    Colour errors are per channel of the NRGBA bytes, as fractions of full
+    scale (1/255 = one step): max_err is the largest, mean_err the mean over
+    every channel of every pixel. winner_mismatch_frac is the fraction of
+    pixels whose last updating element differs, depth_mismatch_frac the
+    fraction whose FP64 depth differs in any bit. With `shaded` (the FP64 /
+    FP32 shader output the GPU kept per pixel), shaded_max_err is the largest
+    per-channel difference from the oracle's FP64 shader output over the
+    pixels whose winners agree and whose values are finite."""
+    img = np.asarray(image, dtype=np.uint8)
+    rc = ref.color()
+    diff = np.abs(img.astype(np.int16) - rc.astype(np.int16))
+    npx = img.shape[0] * img.shape[1]
+    gw, rw = np.asarray(winner), ref.winner()
+    gd = np.ascontiguousarray(depth, dtype=np.float64).view(np.uint64)
+    rd = ref.depth().view(np.uint64)
+    out = {
+        "pixels": int(npx),
+        "max_err": round(float(diff.max(initial=0)) / 255.0, 6),
+        "mean_err": float("%.3g" % (float(diff.mean()) / 255.0)) if diff.size else 0.0,
+        "max_err_steps": int(diff.max(initial=0)),
+        "channels_off": int((diff != 0).sum()),
+        "winner_mismatch_frac": float(int((gw != rw).sum())) / max(npx, 1),
+        "depth_mismatch_frac": float(int((gd != rd).sum())) / max(npx, 1),
+    }
+    if shaded is not None:
+        gs, rs = np.asarray(shaded, dtype=np.float64), ref.shaded()
+        ok = (gw == rw)[..., None] & np.isfinite(gs) & np.isfinite(rs)
+        d = np.abs(gs - rs)[ok]
+        out["shaded_max_err"] = float("%.3g" % float(d.max(initial=0.0)))
+        out["shaded_mean_err"] = float("%.3g" % float(d.mean())) if d.size else 0.0
+    return out
+
+
 def downsample(img, scale):
     """Box downsample of an (H, W, 4) uint8 image (the project's definition)."""
     lib = load()

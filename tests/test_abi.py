@@ -61,6 +61,8 @@ def test_defaults_without_gpu(lib):
     assert list(sh.ambient_color) == [0.2, 0.2, 0.2, 1.0] and list(sh.diffuse_color) == [0.8, 0.8, 0.8, 1.0]
     declared = int(re.search(r"#define FGC_ABI_VERSION (\d+)", open(HEADER).read()).group(1))
     assert lib.fgc_abi_version() == declared
+    # the Python-side defaults (used where the library must not be mapped) agree
+    assert bytes(_abi.state_default()) == bytes(st)
 
 
 def test_argument_errors_without_gpu(lib):

@@ -3,7 +3,9 @@ library allocate device memory once they run (a render service that
 reserves every buffer before admitting work, a host application that owns
 its plugins' GPU memory). fgc_depth_image grows device staging buffers on
 first use; the no-allocation variant keeps that scratch in one static 16 MiB
-device array instead, which limits it to 2^23-pixel frames.
+device array instead, which limits it to 2^23-pixel frames. That array, and
+the kernels the call launches, are made resident when the first context on a
+GPU is created, so the call itself leaves the device's free memory unchanged.
 
 This file is collected last so that, if it fails, a run that stops at the
 first failure has already run every other test."""
@@ -45,6 +47,21 @@ def test_noalloc_depth_image_matches_depth_image_twice(gpu_lib):
         got = noalloc_image(gpu_lib, ctx)
         assert np.array_equal(got, expect)
         assert len(np.unique(got)) > 100  # a real depth gradient, not a constant image
+
+
+def test_noalloc_depth_image_leaves_free_memory_unchanged(gpu_lib):
+    import torch
+    ctx = NewContext(512, 384)
+    draw_frame(ctx, scenes.displaced_sphere(3), scenes.EYE)  # the draw's own buffers exist before the check
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    got = noalloc_image(gpu_lib, ctx)
+    got2 = noalloc_image(gpu_lib, ctx)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, "the call changed free device memory by %d bytes" % (free0 - free1)
+    assert np.array_equal(got, got2)
+    assert np.array_equal(got, ctx.DepthImage())
 
 
 def test_noalloc_depth_image_rejects_frames_above_its_limit(gpu_lib):
