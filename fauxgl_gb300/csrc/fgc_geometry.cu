@@ -89,6 +89,50 @@ __device__ void make_prim(const GeomParams& P, uint64_t slot, D3 s0, D3 s1, D3 s
     R.a0 = a12; R.a1 = a20; R.a2 = a01;
     R.b0 = b12; R.b1 = b20; R.b2 = b01;
     const double area2 = edge_fn(s0, s1, s2);
+    // Rows and columns of the box that hold no covered pixel centre.
+    // rasterize walks rows y0 = floor(min y) .. y1 = ceil(max y) and columns
+    // up to x1 = ceil(max x) (context.go:155-160, 184-207), so its last row
+    // and column (and often the first row) lie wholly beyond the triangle.
+    // The walk's edge values differ from the exact edge functions of the
+    // FP64 screen positions by at most delta = 2^-53 (8 + 6n) (D + 2)^2,
+    // n = D + 4 serial adds, D = box width + height >= the longest edge: the
+    // first value's products and differences, then one rounding per add and
+    // the increments' own rounding. A point whose computed tests all pass
+    // thus has barycentrics >= -delta / |2A| and lies within
+    // 3 delta D / |2A| of the triangle (area A). When 6 delta D <= eps |2A|,
+    // a pixel centre more than eps above min y, below max y or right of max x
+    // is outside in the reference's arithmetic as well, and its row or column
+    // can be left out: the first row moves down when frac(min y) > 1/2 + eps
+    // (the edge values step to it by the reference's own row adds), the last
+    // row is the last centre at or above max y + eps, the last column the
+    // last centre at or left of max x + eps. Outputs are unchanged; the walk
+    // visits fewer rows and pixels. Boxes beyond the bound keep every row.
+    int64_t ry0 = y0, ry1 = y1, rx1 = x1;
+    {
+        constexpr double kEps = 0.00390625;            // 2^-8 pixel
+        constexpr double kHalfEps = 0.5 + kEps;
+        const float D = (float)((x1 - x0) + (y1 - y0));
+        const float n = D + 4.0f;
+        const float lhs = 6.0f * 1.1102230246251565e-16f * (8.0f + 6.0f * n) * (D + 2.0f) * (D + 2.0f) * D;
+        const float rhs = (float)kEps * f32_trunc_pos(dbits(area2) & kAbsMask);  // <= eps |2A|
+        if (dfinite(area2) && rhs > 0.0f && lhs * 1.01f <= rhs) {
+            const double ymin = go_min_i(s0.y, go_min_i(s1.y, s2.y));
+            const double ymax = go_max_i(s0.y, go_max_i(s1.y, s2.y));
+            const double xmax = go_max_i(s0.x, go_max_i(s1.x, s2.x));
+            if (dgt_i(__dsub_rn(ymin, i2d_i(y0)), kHalfEps)) ry0 = y0 + 1;
+            ry1 = y1 - 1 - (dgt_i(__dsub_rn(i2d_i(y1), ymax), kHalfEps) ? 1 : 0);
+            rx1 = x1 - 1 - (dgt_i(__dsub_rn(i2d_i(x1), xmax), kHalfEps) ? 1 : 0);
+            if (ry0 > ry1 || rx1 < x0) {
+                write_dead(P, slot);  // no pixel centre can be covered
+                return;
+            }
+            if (ry0 > y0) {  // w00 += b12 etc. (context.go:275-277) for the row left out
+                R.w0 = __dadd_rn(R.w0, b12);
+                R.w1 = __dadd_rn(R.w1, b20);
+                R.w2 = __dadd_rn(R.w2, b01);
+            }
+        }
+    }
     R.ra = __drcp_rn(area2);  // 1 / x, correctly rounded
     R.q0 = __drcp_rn(a12);
     R.q1 = __drcp_rn(a20);
@@ -98,7 +142,7 @@ __device__ void make_prim(const GeomParams& P, uint64_t slot, D3 s0, D3 s1, D3 s
     R.v0 = v0; R.v1 = v1; R.v2 = v2;
     R.elem = elem;
     P.prims[slot] = R;
-    P.pbox[slot] = PBox{(int32_t)x0, (int32_t)x1, (int32_t)y0, (int32_t)y1};
+    P.pbox[slot] = PBox{(int32_t)x0, (int32_t)rx1, (int32_t)ry0, (int32_t)ry1};
     P.rf[slot] = make_float4((float)r0, (float)r1, (float)r2, 0.0f);
     // A row's covered pixel centres lie on one horizontal chord of the
     // triangle, so a row holds at most (widest chord) + 1 of them; +3 more
@@ -110,7 +154,7 @@ __device__ void make_prim(const GeomParams& P, uint64_t slot, D3 s0, D3 s1, D3 s
     // chunk the bound does not hold for, so it affects speed only.
     const unsigned long long h01 = dbits(a01) & kAbsMask, h12 = dbits(a12) & kAbsMask, h20 = dbits(a20) & kAbsMask;
     const unsigned long long hb = h01 > h12 ? (h01 > h20 ? h01 : h20) : (h12 > h20 ? h12 : h20);
-    const uint32_t bw = (uint32_t)(x1 - x0 + 1);
+    const uint32_t bw = (uint32_t)(rx1 - x0 + 1);
     uint32_t span = bw;
     if (hb != 0) {
         const float chord = f32_trunc_pos(dbits(area2) & kAbsMask) / f32_trunc_pos(hb);

@@ -241,6 +241,39 @@ def test_odd_frame_shapes(gpu_lib, w, h):
     p.check()
 
 
+def test_boxes_at_pixel_centre_boundaries(gpu_lib):
+    """Triangles whose extremes sit on, just inside or just outside pixel
+    centres (offsets of 0, 1e-15, 1e-9, 2^-8 and 2^-8 +- 1e-12 around
+    k + 1/2), needles and slivers: the setup leaves out box rows and columns
+    that hold no covered centre, and the frame must not change."""
+    rng = np.random.default_rng(2024)
+    w = h = 96
+    offs = np.array([0.0, 1e-15, -1e-15, 1e-9, -1e-9, 2.0 ** -8, -2.0 ** -8, 2.0 ** -8 + 1e-12,
+                     -2.0 ** -8 - 1e-12, 2.0 ** -8 - 1e-12, 0.25, -0.25, 0.499, 0.501])
+    tris = []
+    for _ in range(1500):
+        c = rng.integers(4, w - 8, size=2)
+        pts = []
+        for _ in range(3):
+            d = rng.integers(-3, 4, size=2)
+            o = rng.choice(offs, size=2)
+            pts.append((float(c[0] + d[0]) + 0.5 + o[0], float(c[1] + d[1]) + 0.5 + o[1]))
+        tris.append(pts)
+    for _ in range(300):  # needles and slivers: two corners almost together
+        x, y = rng.uniform(4, w - 8, size=2)
+        dx, dy = rng.uniform(-6, 6, size=2)
+        e = rng.choice([1e-13, 1e-9, 1e-6, 1e-3])
+        tris.append([(x, y), (x + dx, y + dy), (x + dx + e, y + dy - e)])
+    mesh = screen_triangle_mesh(tris, w, h)
+    p = Pair(w, h)
+    for prec in (_abi.FGC_PRECISION_PLAIN, _abi.FGC_PRECISION_MIXED):
+        for st in (state(cull=_abi.FGC_CULL_NONE, precision=prec),
+                   state(cull=_abi.FGC_CULL_NONE, wireframe=1, line_width=0.75, precision=prec)):
+            p = Pair(w, h)
+            run_both(p, mesh, st, solid((0.3, 0.6, 0.9, 0.7)))
+            p.check(mixed=prec == _abi.FGC_PRECISION_MIXED)
+
+
 def test_triangle_and_line_ranges(gpu_lib):
     mesh = random_scene(5, ntri=90, nline=40)
     m = scene_matrix(1.0)
