@@ -92,6 +92,10 @@ int fill_views(const fgc_state* st, const fgc_shader* sh, StateView& sv, ShaderV
     if (shv.power >= 2 && shv.power < 9223372036854775808.0 && shv.power == std::trunc(shv.power))
         shv.pow_yi = (uint64_t)shv.power;
     shv.object_is_discard = (sh->color[0] == 0 && sh->color[1] == 0 && sh->color[2] == 0 && sh->color[3] == 0);
+    // equal channels give equal light channels: the shader then computes one
+    auto same3 = [](const double* c) { return memcmp(&c[0], &c[1], 8) == 0 && memcmp(&c[0], &c[2], 8) == 0; };
+    shv.gray_light = same3(shv.ambient) && same3(shv.diffuse) ? 1 : 0;
+    shv.gray_spec = same3(shv.specular) ? 1 : 0;
     if (sh->texture) {
         shv.has_texture = 1;
         shv.tex.texels = sh->texture->texels.p;

@@ -120,6 +120,8 @@ struct ShaderView {
     int32_t has_texture;
     int32_t object_is_discard;  // PhongShader: ObjectColor == Discard
     int32_t power_pos;          // SpecularPower > 0 (the Fragment's test, made once)
+    int32_t gray_light;         // AmbientColor and DiffuseColor each have equal R, G, B (bit for bit)
+    int32_t gray_spec;          // SpecularColor has equal R, G, B
     double m[16];
     double color[4];
     double light[3];

@@ -77,9 +77,14 @@ __device__ void make_prim(const GeomParams& P, uint64_t slot, D3 s0, D3 s1, D3 s
     }
     D3 p = d3(__dadd_rn(i2d_i(x0), 0.5), __dadd_rn(i2d_i(y0), 0.5), 0.0);  // |x0|, |y0| <= 2^30 here
     RPrim R;
-    R.w0 = edge_fn(s1, s2, p);
-    R.w1 = edge_fn(s2, s0, p);
-    R.w2 = edge_fn(s0, s1, p);
+    // edge(a, b, p) = (b.X - p.X)(a.Y - p.Y) - (b.Y - p.Y)(a.X - p.X)
+    // (context.go:147-149): the six differences to p are shared by the three
+    // edges
+    const double dx0 = __dsub_rn(s0.x, p.x), dx1 = __dsub_rn(s1.x, p.x), dx2 = __dsub_rn(s2.x, p.x);
+    const double dy0 = __dsub_rn(s0.y, p.y), dy1 = __dsub_rn(s1.y, p.y), dy2 = __dsub_rn(s2.y, p.y);
+    R.w0 = __dsub_rn(__dmul_rn(dx2, dy1), __dmul_rn(dy2, dx1));  // edge(s1, s2, p)
+    R.w1 = __dsub_rn(__dmul_rn(dx0, dy2), __dmul_rn(dy0, dx2));  // edge(s2, s0, p)
+    R.w2 = __dsub_rn(__dmul_rn(dx1, dy0), __dmul_rn(dy1, dx0));  // edge(s0, s1, p)
     double a01 = __dsub_rn(s1.y, s0.y);
     double b01 = __dsub_rn(s0.x, s1.x);
     double a12 = __dsub_rn(s2.y, s1.y);
@@ -88,7 +93,10 @@ __device__ void make_prim(const GeomParams& P, uint64_t slot, D3 s0, D3 s1, D3 s
     double b20 = __dsub_rn(s2.x, s0.x);
     R.a0 = a12; R.a1 = a20; R.a2 = a01;
     R.b0 = b12; R.b1 = b20; R.b2 = b01;
-    const double area2 = edge_fn(s0, s1, s2);
+    // edge(s0, s1, s2) = (s1.X - s2.X)(s0.Y - s2.Y) - (s1.Y - s2.Y)(s0.X - s2.X):
+    // its factors are b12, a20, -a12 and -b20 (a rounded difference changes
+    // only its sign when the operands swap), and (-a12)(-b20) = a12 b20
+    const double area2 = __dsub_rn(__dmul_rn(b12, a20), __dmul_rn(a12, b20));
     // Rows and columns of the box that hold no covered pixel centre.
     // rasterize walks rows y0 = floor(min y) .. y1 = ceil(max y) and columns
     // up to x1 = ceil(max x) (context.go:155-160, 184-207), so its last row

@@ -276,8 +276,8 @@ constexpr int kRasterHeads = 2048;
 constexpr int kBandRowsMax = 128;
 
 // (primitive, row) units a chunk of wide primitives holds: kSpanUnitsMax
-// where shared memory allows it without a smaller fragment buffer, else
-// kSpanUnitsMin. A primitive with more rows in a band than a chunk holds
+// (the span arrays then also hold the narrow walk's warp queues) unless
+// shared memory cannot hold it, else kSpanUnitsMin. A primitive with more rows in a band than a chunk holds
 // (wrap-around rows of a box beyond the frame's sides) is split over chunks.
 constexpr int kSpanUnitsMin = 128;
 constexpr int kSpanUnitsMax = 256;

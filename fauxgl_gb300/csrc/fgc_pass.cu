@@ -105,7 +105,10 @@ int fit_fragments(const DevLimits& D, const PassTuning& T, int precision, int32_
     const long two_cta = (long)D.smem_per_sm / 2 - D.smem_reserved_per_block - stat;
     const long one_cta = (long)D.smem_per_block_optin - stat;
     F = std::max(256, std::min(T.frag_cap, 4096));
-    su = kSpanUnitsMin;
+    // the larger span arrays first: they also hold the warp queues of the
+    // narrow walk, which needs one 32-entry queue per warp (kSpanUnitsMax =
+    // the CTA's threads) and is worth more than a larger fragment buffer
+    su = kSpanUnitsMax;
     smem = raster_smem_bytes(Lmax, F, kRasterThreads, su);
     // two CTAs per SM (the register budget allows two) when a smaller
     // fragment buffer makes them fit
@@ -117,14 +120,12 @@ int fit_fragments(const DevLimits& D, const PassTuning& T, int precision, int32_
         F /= 2;
         smem = raster_smem_bytes(Lmax, F, kRasterThreads, su);
     }
-    if ((long)smem > one_cta) return fail(FGC_ERR_UNSUPPORTED, "frame too wide for the band rasteriser");
-    // the larger span chunk where it costs neither fragments nor a CTA per SM
-    const long budget = (long)smem <= two_cta ? two_cta : one_cta;
-    const size_t wide = raster_smem_bytes(Lmax, F, kRasterThreads, kSpanUnitsMax);
-    if ((long)wide <= budget) {
-        su = kSpanUnitsMax;
-        smem = wide;
+    if ((long)smem > one_cta) {
+        // the smaller span arrays (narrow rows then walk thread by thread)
+        su = kSpanUnitsMin;
+        smem = raster_smem_bytes(Lmax, F, kRasterThreads, su);
     }
+    if ((long)smem > one_cta) return fail(FGC_ERR_UNSUPPORTED, "frame too wide for the band rasteriser");
     return FGC_OK;
 }
 

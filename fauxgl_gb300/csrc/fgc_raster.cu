@@ -189,10 +189,18 @@ __device__ D4 shade64(const RasterParams& P, const ItemView& I, const RPrim& R, 
         color = bilinear64(S.tex, interp1(u0, u1, u2, w), interp1(v0, v1, v2, w));
     }
     D3 L = d3(S.light[0], S.light[1], S.light[2]);
-    D4 light = d4(S.ambient[0], S.ambient[1], S.ambient[2], S.ambient[3]);
     const double ndl = dot3(nrm, L);
     double diffuse = go_max0(ndl);
-    light = add4(light, muls4(d4(S.diffuse[0], S.diffuse[1], S.diffuse[2], S.diffuse[3]), diffuse));
+    // light = AmbientColor + DiffuseColor * diffuse (its alpha never reaches
+    // the result); with equal R, G, B inputs the three channels are equal
+    D3 light;
+    light.x = __dadd_rn(S.ambient[0], __dmul_rn(S.diffuse[0], diffuse));
+    if (S.gray_light) {
+        light.y = light.z = light.x;
+    } else {
+        light.y = __dadd_rn(S.ambient[1], __dmul_rn(S.diffuse[1], diffuse));
+        light.z = __dadd_rn(S.ambient[2], __dmul_rn(S.diffuse[2], diffuse));
+    }
     if (dgt0(diffuse) && S.power_pos) {
         // the interpolated position is read only here
         const D3 pos = d3(interp1(p0.x, p1.x, p2.x, w), interp1(p0.y, p1.y, p2.y, w), interp1(p0.z, p1.z, p2.z, w));
@@ -207,7 +215,17 @@ __device__ D4 shade64(const RasterParams& P, const ItemView& I, const RPrim& R, 
         double specular = go_max0(dot3(camera, reflected));
         if (dgt0(specular)) {
             specular = pow_specular(specular, S.power, S.pow_yi);
-            light = add4(light, muls4(d4(S.specular[0], S.specular[1], S.specular[2], S.specular[3]), specular));
+            const double s0 = __dmul_rn(S.specular[0], specular);
+            if (S.gray_light && S.gray_spec) {
+                light.x = __dadd_rn(light.x, s0);
+                light.y = light.z = light.x;
+            } else {
+                const double s1 = S.gray_spec ? s0 : __dmul_rn(S.specular[1], specular);
+                const double s2 = S.gray_spec ? s0 : __dmul_rn(S.specular[2], specular);
+                light.x = __dadd_rn(light.x, s0);
+                light.y = __dadd_rn(light.y, s1);
+                light.z = __dadd_rn(light.z, s2);
+            }
         }
     }
     return d4(go_min1(__dmul_rn(color.x, light.x)), go_min1(__dmul_rn(color.y, light.y)),
