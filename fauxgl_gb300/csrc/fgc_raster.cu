@@ -702,16 +702,26 @@ __device__ __forceinline__ void flush_queued(uint32_t n, uint32_t q0, double ra,
     const double z0i = __shfl_sync(0xffffffffu, z0, src);
     const double z1i = __shfl_sync(0xffffffffu, z1, src);
     const double z2i = __shfl_sync(0xffffffffu, z2, src);
-    if (lane >= n) return;
-    const uint32_t key = (uint32_t)S.ux[e];
-    const uint32_t pix = key >> 16;
-    const double b0 = __dmul_rn(S.uw0[e], rai);
-    const double b1 = __dmul_rn(S.uw1[e], rai);
-    const double b2 = __dmul_rn(S.uw2[e], rai);
-    const double z = __dadd_rn(__dadd_rn(__dmul_rn(b0, z0i), __dmul_rn(b1, z1i)), __dmul_rn(b2, z2i));
-    const double bias = I.st.depth_bias;
-    if (B.early && dgt_i(add_bias(z, bias, dbits(bias) == 0), S.depth[pix])) return;
-    const uint32_t slot = atomicAdd(s_nfrag, 1u);
+    uint32_t key = 0, pix = 0;
+    double b0 = 0, b1 = 0, b2 = 0, z = 0;
+    bool keep = false;
+    if (lane < n) {
+        key = (uint32_t)S.ux[e];
+        pix = key >> 16;
+        b0 = __dmul_rn(S.uw0[e], rai);
+        b1 = __dmul_rn(S.uw1[e], rai);
+        b2 = __dmul_rn(S.uw2[e], rai);
+        z = __dadd_rn(__dadd_rn(__dmul_rn(b0, z0i), __dmul_rn(b1, z1i)), __dmul_rn(b2, z2i));
+        const double bias = I.st.depth_bias;
+        keep = !(B.early && dgt_i(add_bias(z, bias, dbits(bias) == 0), S.depth[pix]));
+    }
+    // one fragment-slot allocation for the warp's kept pixels, in lane order
+    const uint32_t km = __ballot_sync(0xffffffffu, keep);
+    uint32_t base = 0;
+    if (lane == 0 && km) base = atomicAdd(s_nfrag, (uint32_t)__popc(km));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (!keep) return;
+    const uint32_t slot = base + (uint32_t)__popc(km & ((1u << lane) - 1u));
     if (slot >= (uint32_t)P.F) {
         atomicOr(s_conflict, 2u);
         return;
@@ -888,8 +898,23 @@ __device__ __forceinline__ void emit_segment(const RPrim& R, const ItemView& I, 
 // ---------------------------------------------------------------------------
 // Resolve
 // ---------------------------------------------------------------------------
+// The colour of the pixel a resolve thread is applying fragments to, held in
+// a register between fragments of the same pixel: one load (when a blend
+// needs it) and one store per pixel instead of a global read-modify-write
+// per fragment. One thread applies all of a pixel's fragments, in order.
+struct ColorCache {
+    uint32_t* p;  // the cached pixel's colour, or null
+    uint32_t v;
+    bool loaded, dirty;
+};
+__device__ __forceinline__ void cc_flush(ColorCache& cc) {
+    if (cc.p && cc.dirty) *cc.p = cc.v;
+    cc.p = nullptr;
+    cc.dirty = false;
+}
+
 __device__ __forceinline__ void apply_fragment(const RasterParams& P, const ItemView& I, const BandCtx& B,
-                                               RasterSmem& S, uint32_t f, uint64_t& updated) {
+                                               RasterSmem& S, uint32_t f, uint64_t& updated, ColorCache& cc) {
     const uint8_t fl = S.fflag[f];
     if (fl & kFragDiscard) return;
     const uint32_t key = S.fkey[f];
@@ -904,13 +929,27 @@ __device__ __forceinline__ void apply_fragment(const RasterParams& P, const Item
             // The colour buffer stays in global memory: the band is this
             // CTA's alone and one thread applies all of a pixel's fragments.
             uint32_t* cp = I.color + B.i0 + pix;
+            if (cc.p != cp) {
+                cc_flush(cc);
+                cc.p = cp;
+                cc.loaded = false;
+            }
             if (fl & kFragBlend) {
-                *cp = blend_nrgba(*cp, S.fcol[f]);
+                if (!cc.loaded) {
+                    cc.v = *cp;
+                    cc.loaded = true;
+                }
+                cc.v = blend_nrgba(cc.v, S.fcol[f]);
+                cc.dirty = true;
             } else {
                 // SetNRGBA(x, y, c) ignores points outside the image rectangle:
                 // x = i - y*W with i = r0*W + pix
                 const int32_t x = pix - (S.urow[unit] - B.r0) * I.W;
-                if (x >= 0 && x < I.W) *cp = S.fcol[f];
+                if (x >= 0 && x < I.W) {
+                    cc.v = S.fcol[f];
+                    cc.loaded = true;
+                    cc.dirty = true;
+                }
             }
         }
         if (I.winner) {
@@ -962,19 +1001,66 @@ __device__ __forceinline__ void shade_fragment(const RasterParams& P, const Item
 }
 
 // Apply the chunk's fragments per pixel in (primitive, row) order. Every
-// fragment was pushed onto its pixel bucket's list in A1 (head / nxt).
-// Without collisions each list has one entry and all apply in parallel;
-// otherwise the thread holding a list's head applies the bucket's fragments
-// by increasing key -- pixel, then unit -- selecting the next key from the
-// short list each time. The lists are emptied for the next chunk as they are
-// applied.
+// fragment was pushed onto its pixel bucket's list when it was recorded
+// (head / nxt). Without collisions each list has one entry and all apply in
+// parallel. Otherwise every fragment counts, on its bucket's list, the
+// fragments of its own pixel with a smaller key (pixel, then unit): that
+// rank goes into the upper bits of its flags, and rounds r = 0, 1, ... apply
+// the fragments of rank r in parallel (one per pixel per round). A pixel
+// with more fragments in the chunk than the rank field holds sends the chunk
+// to the serial form: the thread holding a list's head applies the bucket's
+// fragments by increasing key, selecting the next key from the list each
+// time. The lists are emptied for the next chunk afterwards.
+constexpr int kRankShift = 2;
+constexpr uint32_t kRankMax = 62;
+
 __device__ void resolve_chunk(const RasterParams& P, const ItemView& I, const BandCtx& B, RasterSmem& S,
-                              uint32_t nfrag, bool conflict, uint64_t& updated) {
+                              uint32_t nfrag, bool conflict, uint64_t& updated, uint32_t* s_rank) {
+    ColorCache cc{nullptr, 0u, false, false};
     if (!conflict) {
         for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) {
-            apply_fragment(P, I, B, S, f, updated);
+            apply_fragment(P, I, B, S, f, updated, cc);
+            cc_flush(cc);
             S.head[bucket_of(S.fkey[f] >> 16)] = 0xFFFFu;
         }
+        return;
+    }
+    if (threadIdx.x == 0) *s_rank = 0;
+    __syncthreads();
+    uint32_t mymax = 0;
+    for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) {
+        const uint32_t key = S.fkey[f], pix = key >> 16;
+        uint32_t r = 0, steps = 0;
+        // A list holds at most nfrag entries; every traversal is capped at
+        // that, and a list that does not end within it is reported instead
+        // of followed.
+        for (uint32_t g = S.head[bucket_of(pix)]; g != 0xFFFFu && g < nfrag; g = S.nxt[g]) {
+            if (++steps > nfrag) {
+                atomicOr(P.status, ST_RASTER_INTERNAL);
+                break;
+            }
+            const uint32_t k = S.fkey[g];
+            r += ((k >> 16) == pix && k < key) ? 1u : 0u;
+        }
+        if (r > kRankMax + 1) r = kRankMax + 1;
+        S.fflag[f] = (uint8_t)((S.fflag[f] & ((1u << kRankShift) - 1u)) | (r << kRankShift));
+        mymax = max(mymax, r);
+    }
+    for (int o = 16; o > 0; o >>= 1) mymax = max(mymax, __shfl_xor_sync(0xffffffffu, mymax, o));
+    if ((threadIdx.x & 31) == 0 && mymax) atomicMax(s_rank, mymax);
+    __syncthreads();
+    const uint32_t maxr = *s_rank;
+    if (maxr <= kRankMax) {
+        for (uint32_t r = 0; r <= maxr; r++) {
+            for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) {
+                if ((uint32_t)(S.fflag[f] >> kRankShift) == r) {
+                    apply_fragment(P, I, B, S, f, updated, cc);
+                    cc_flush(cc);
+                }
+            }
+            __syncthreads();
+        }
+        for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) S.head[bucket_of(S.fkey[f] >> 16)] = 0xFFFFu;
         return;
     }
     for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) {
@@ -982,9 +1068,6 @@ __device__ void resolve_chunk(const RasterParams& P, const ItemView& I, const Ba
         if (S.head[pix] != f) continue;  // not the list head
         uint32_t last = 0;               // keys in a bucket are distinct
         bool first = true;
-        // A list holds at most nfrag entries; every traversal is capped at
-        // that, and a list that does not end within it is reported instead
-        // of followed.
         for (uint32_t picked = 0; picked < nfrag; picked++) {
             uint32_t best = 0xFFFFFFFFu, bestf = 0xFFFFu, steps = 0;
             for (uint32_t g = f; g != 0xFFFFu && g < nfrag; g = S.nxt[g]) {
@@ -999,12 +1082,14 @@ __device__ void resolve_chunk(const RasterParams& P, const ItemView& I, const Ba
                 }
             }
             if (bestf == 0xFFFFu) break;
-            apply_fragment(P, I, B, S, bestf, updated);
+            apply_fragment(P, I, B, S, bestf, updated, cc);
             last = best;
             first = false;
         }
-        S.head[pix] = 0xFFFFu;
+        cc_flush(cc);
     }
+    __syncthreads();  // every list walked before any head is cleared
+    for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) S.head[bucket_of(S.fkey[f] >> 16)] = 0xFFFFu;
 }
 
 // ---------------------------------------------------------------------------
@@ -1141,7 +1226,8 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
         S.nxt = (unsigned short*)q; q += (size_t)F * 2;
         S.fflag = (uint8_t*)q;
     }
-    __shared__ uint32_t s_band, s_item, s_nfrag, s_conflict, s_nprim, s_nunit, s_ftotal, s_mode, s_bsum, s_ratio, s_split;
+    __shared__ uint32_t s_band, s_item, s_nfrag, s_conflict, s_nprim, s_nunit, s_ftotal, s_mode, s_bsum, s_ratio, s_split,
+        s_rank;
     __shared__ uint64_t s_warp[kRT / 32 + 1];
     __shared__ ItemView s_iv;  // the draw of the current band
     const ItemView& I = s_iv;
@@ -1332,7 +1418,7 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
                     }
                     for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) shade_fragment<PREC>(P, I, S, f);
                     __syncthreads();
-                    resolve_chunk(P, I, B, S, nfrag, (s_conflict & 1u) != 0, upd);
+                    resolve_chunk(P, I, B, S, nfrag, (s_conflict & 1u) != 0, upd, &s_rank);
                 }
                 __syncthreads();
                 if (redo && level < 2) {
@@ -1438,7 +1524,7 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
                 if (threadIdx.x == 0) shd += nfrag;
                 for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) shade_fragment<PREC>(P, I, S, f);
                 __syncthreads();
-                resolve_chunk(P, I, B, S, nfrag, (s_conflict & 1u) != 0, upd);
+                resolve_chunk(P, I, B, S, nfrag, (s_conflict & 1u) != 0, upd, &s_rank);
                 __syncthreads();
             }
             if (split) {
