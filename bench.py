@@ -73,7 +73,8 @@ def parse():
     ap.add_argument("--batch-tuning", default="auto",
                     help="'auto' (autotune) or band_pixels,prims_per_bin_block,fragment_cap,window")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per rate of the serving loop")
-    ap.add_argument("--serve-max-requests", type=int, default=160, help="requests per rate at most")
+    ap.add_argument("--serve-timeout", type=float, default=1.0,
+                    help="seconds a serving request may wait for admission before it is shed")
     ap.add_argument("--serve-budget-gb", type=int, default=96, help="HBM budget of the serving loop")
     ap.add_argument("--only", choices=["all", "plain", "mixed", "ss16", "batch", "serve", "meshprep", "accuracy"],
                     default="all",
@@ -500,20 +501,33 @@ def bench_meshprep(lib, mesh, torch, cpu=True):
     return out
 
 
-SERVE_WORKLOAD = ("serving loop: pool of 64 resident meshes (displaced icospheres, 5k-1.31M triangles log-uniform, "
-                  "seed 4), Poisson arrivals, each request a random mesh, camera at radius 3, resolution in "
-                  "{512^2, 1920x1080, 3840x2160}, supersampling scale in {1, 2, 4} (box-downsampled on the "
-                  "device, result copied to the host), PhongShader with a random object colour")
+SERVE_WORKLOAD = ("serving loop: pool of 64 resident meshes built as the dense and thumbnail workloads build them "
+                  "(displaced icospheres of 5k-1.31M triangles log-uniform, capped cylinders and cones with 8-512 "
+                  "segments; seed 4), "
+                  "Poisson arrivals over the whole window at each rate, each request a random mesh, camera at "
+                  "radius 3, resolution in {512^2, 1920x1080, 3840x2160}, supersampling scale in {1, 2, 4} "
+                  "(box-downsampled on the device, result copied to the host), PhongShader with a random object "
+                  "colour; requests waiting longer than the request timeout are shed")
 
 
 def _pool_mesh(args):
     from fauxgl_gb300 import scenes
-    detail, seed = args
-    return scenes.displaced_sphere(detail, seed=seed)
+    from fauxgl_gb300.shapes import cylinder_segments
+    kind, size, seed = args
+    if kind == "sphere":
+        m = scenes.displaced_sphere(size, seed=seed)
+    else:
+        m = cylinder_segments(size, capped=True, cone=(kind == "cone"))
+        m.BiUnitCube()
+    m.kind = kind
+    return m
 
 
 def serve_pool(n=64, seed=4, tri_min=5000, tri_max=1310720):
-    """The serving workload's resident meshes, built on all host cores."""
+    """The serving workload's resident meshes, built on all host cores as the
+    dense and thumbnail workloads build theirs: displaced icospheres at the
+    subdivision nearest a triangle count drawn log-uniform from
+    [tri_min, tri_max], and capped cylinders and cones with 8-512 segments."""
     import math
     import multiprocessing as mp
     from fauxgl_gb300 import scenes
@@ -521,9 +535,14 @@ def serve_pool(n=64, seed=4, tri_min=5000, tri_max=1310720):
     jobs = []
     for i in range(n):
         t = math.exp(math.log(tri_min) + rng.uniform() * (math.log(tri_max) - math.log(tri_min)))
-        detail = int(min(8, max(2, round(math.log(t / 20.0, 4)))))
-        jobs.append((detail, seed * 1000003 + i))
-    order = sorted(range(n), key=lambda i: -jobs[i][0])  # biggest first
+        kind = ("sphere", "cylinder", "cone")[int(rng.uniform() * 3)]
+        if kind == "sphere":
+            size = int(min(8, max(2, round(math.log(t / 20.0, 4)))))
+        else:
+            size = int(math.exp(math.log(8) + rng.uniform() * (math.log(512) - math.log(8))))
+        jobs.append((kind, size, seed * 1000003 + i))
+    weight = [20 * 4 ** j[1] if j[0] == "sphere" else j[1] for j in jobs]
+    order = sorted(range(n), key=lambda i: -weight[i])  # biggest first
     with mp.get_context("spawn").Pool(min(n, os.cpu_count() or 1)) as p:
         built = p.map(_pool_mesh, [jobs[i] for i in order], chunksize=1)
     meshes = [None] * n
@@ -555,25 +574,52 @@ def serve_requests(meshes, n, seed):
 
 
 def bench_serve(args, meshes):
-    """Config-4 serving loop at each arrival rate, mixed and plain forms."""
+    """Config-4 serving loop, mixed and plain forms: the saturation throughput
+    of a closed loop (the queue never runs dry), then each offered rate over
+    its whole arrival window with load shedding (requests that wait longer
+    than the request timeout expire)."""
     from fauxgl_gb300 import _abi
     from fauxgl_gb300.serve import Server, latency_summary, poisson_arrivals, run_load
     rates = [50, 200, 500, 1000, 2000]
-    out = {"workload": SERVE_WORKLOAD, "pool_triangles": sum(m.ntri for m in meshes), "rates": {}}
+    out = {"workload": SERVE_WORKLOAD, "pool_triangles": sum(m.ntri for m in meshes),
+           "pool_kinds": {k: sum(1 for m in meshes if getattr(m, "kind", None) == k)
+                          for k in ("sphere", "cylinder", "cone")},
+           "window_s": args.serve_seconds, "request_timeout_s": args.serve_timeout, "saturation": {}, "rates": {}}
     for form, prec in (("mixed", _abi.FGC_PRECISION_MIXED), ("plain", _abi.FGC_PRECISION_PLAIN)):
-        srv = Server(meshes, hbm_budget=args.serve_budget_gb << 30, slots=3, max_batch=32, precision=prec)
-        # warm-up: one request of each size class
+        srv = Server(meshes, hbm_budget=args.serve_budget_gb << 30, slots=3, max_batch=32, precision=prec,
+                     request_timeout=args.serve_timeout)
         warm = serve_requests(meshes, 6, seed=99)
         run_load(srv, warm, [0.0] * len(warm))
+        # saturation: keep the queue full for the window, after a window of
+        # the same load that creates the contexts the mix needs
+        reqs = iter(serve_requests(meshes, 100000, seed=77))
+        for measured in (False, True):
+            t0 = time.perf_counter()
+            done, frags = 0, 0
+            while time.perf_counter() - t0 < args.serve_seconds:
+                while len(srv.pending) < 2 * srv.max_batch:
+                    srv.submit(next(reqs))
+                for t in srv.poll():
+                    done += 1
+                    frags += t.info[0]
+        el = time.perf_counter() - t0
+        for t in list(srv.pending):  # the queue's remainder is not part of the measurement
+            srv.cancel(t)
+        srv.drain()
+        out["saturation"][form] = {"frames_per_s": round(done / el, 2), "gfragments_per_s": round(frags / el / 1e9, 3),
+                                   "window_s": round(el, 3)}
+        log("serve %s saturation: %s" % (form, out["saturation"][form]))
         res = {}
         for k, rate in enumerate(rates):
-            arr = poisson_arrivals(float(rate), args.serve_seconds, seed=40 + k)[:args.serve_max_requests]
+            arr = poisson_arrivals(float(rate), args.serve_seconds, seed=40 + k)
             reqs = serve_requests(meshes, len(arr), seed=400 + k)
             tickets, elapsed = run_load(srv, reqs, arr)
             lat = latency_summary(tickets)
-            frags = sum(t.info[0] for t in tickets if t.done)
-            res[str(rate)] = {"requests": len(reqs), "elapsed_s": round(elapsed, 3),
-                              "frames_per_s": round(len(tickets) / elapsed, 2),
+            served = [t for t in tickets if t.done]
+            frags = sum(t.info[0] for t in served)
+            res[str(rate)] = {"offered": len(reqs), "served": len(served),
+                              "expired": sum(1 for t in tickets if t.status == "expired"),
+                              "elapsed_s": round(elapsed, 3), "frames_per_s": round(len(served) / elapsed, 2),
                               "gfragments_per_s": round(frags / elapsed / 1e9, 3), **lat}
             log("serve %s %4d req/s: %s" % (form, rate, res[str(rate)]))
         out["rates"][form] = res
@@ -855,7 +901,7 @@ def main():
     info = (plain.info.total_pixels, plain.info.updated_pixels)
     plain.set_timing(False)
 
-    e2e_ms = mixed_ms = None
+    e2e_ms = mixed_ms = e2e_upload = None
     ss = {}
     h2d = ctypes.sizeof(_abi.FgcState) + ctypes.sizeof(_abi.FgcShader) + 2 * 32
     d2h = W * H * 4 + ctypes.sizeof(_abi.FgcRasterizeInfo)
@@ -881,6 +927,37 @@ def main():
         torch.cuda.synchronize()
         barrier()
         e2e_ms = e0.elapsed_time(e1) / args.steps
+
+        # ---- the same with the mesh uploaded every frame (not resident) ----
+        # fgc_mesh_upload from the host arrays (positions + normals), clears,
+        # the draw, the read-back, fgc_mesh_release: what DrawMesh of a mesh
+        # that was not made resident costs
+        tp = np.ascontiguousarray(mesh.tri_pos)
+        tn = np.ascontiguousarray(mesh.tri_nrm)
+        up_steps = max(3, min(args.steps, 5))
+
+        def upload_frame():
+            h = ctypes.c_void_p()
+            _abi.check(lib.fgc_mesh_upload(_abi.dptr(tp), _abi.dptr(tn), None, None, mesh.ntri, None, None, None,
+                                           None, 0, ctypes.byref(h)))
+            plain.mesh_h = h.value
+            plain.run()
+            _abi.check(lib.fgc_read_color(plain.ctx, ptr))
+            _abi.check(lib.fgc_mesh_release(h))
+            plain.mesh_h = mesh_h
+
+        upload_frame()
+        torch.cuda.synchronize()
+        t_up = time.perf_counter()
+        for _ in range(up_steps):
+            upload_frame()
+        torch.cuda.synchronize()
+        upload_ms = (time.perf_counter() - t_up) * 1e3 / up_steps
+        e2e_upload = {"value": round(world * 1e3 / upload_ms, 3), "unit": "frames/s", "steps": up_steps,
+                      "h2d_bytes_per_step": h2d + tp.nbytes + tn.nbytes, "d2h_bytes_per_step": d2h,
+                      "how": "fgc_mesh_upload of the 1,310,720 triangles' positions and normals from pageable host "
+                             "memory, clears, fgc_draw_mesh, fgc_read_color, fgc_mesh_release every frame; host wall "
+                             "time (the upload is synchronous)"}
 
         # ---- mixed form at 1080p --------------------------------------------
         mixed = Frame(lib, mesh_h, W, H, _abi.FGC_PRECISION_MIXED)
@@ -957,7 +1034,8 @@ def main():
                        "l2": "inputs larger than L2 (mesh ~300 MB + framebuffer 25 MB resident; L2 129 MB)",
                        "rasterize_info": list(info)},
             "e2e": ({"value": round(world * 1e3 / e2e_ms, 3), "unit": "frames/s", "h2d_bytes_per_step": h2d,
-                     "d2h_bytes_per_step": d2h} if e2e_ms else None),
+                     "d2h_bytes_per_step": d2h, "mesh": "resident"} if e2e_ms else None),
+            "e2e_upload": e2e_upload,
             "gpu_launches": launches * args.steps,
             "roofline": {"bound": "fp64", "kernel": names[dom] + "_kernel", "achieved": round(achieved, 4),
                          "peak": round(fp64_peak_tflops, 4), "unit": "TFLOP/s",

@@ -178,6 +178,7 @@ SIGNATURES = {
     "fgc_context_set_timing": (_I, [_P, _I32]),
     "fgc_context_last_stats": (_I, [_P, ctypes.POINTER(FgcStats)]),
     "fgc_context_set_stream": (_I, [_P, _P]),
+    "fgc_debug_lookback": (_I, [ctypes.c_uint32, ctypes.c_uint32]),
     "fgc_measure_fp64_rate": (_I, [_D]),
     "fgc_batch_create": (_I, [_PP]),
     "fgc_batch_destroy": (_I, [_P]),

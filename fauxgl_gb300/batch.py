@@ -20,7 +20,7 @@ import ctypes
 import numpy as np
 
 from . import _abi
-from .context import RasterizeInfo, _DeviceHandle, _upload_mesh
+from .context import RasterizeInfo, _DeviceHandle, _draw_handle
 
 
 class Batch:
@@ -57,7 +57,10 @@ class Batch:
         out = None
         if read_back:
             out = np.empty((ctx.Height // scale, ctx.Width // scale, 4), dtype=np.uint8)
-        self._draws.append((ctx, mesh, _upload_mesh(mesh), int(tri_first), int(tri_count), int(line_first),
+        # a mesh that is not resident is copied to the device now (its owner
+        # stays with the draw until the batch is done)
+        handle, owner = _draw_handle(mesh)
+        self._draws.append((ctx, owner or mesh, handle, int(tri_first), int(tri_count), int(line_first),
                             int(line_count), st, sh, out, int(scale)))
         return len(self._draws) - 1
 

@@ -73,6 +73,19 @@ def _upload_mesh(mesh):
     return mesh._device.handle
 
 
+def _draw_handle(mesh):
+    """(device handle, owner) of the mesh for one draw: the kept copy of a
+    DeviceMesh or a resident Mesh (owner None), else a copy uploaded now from
+    the mesh's current arrays and released with its owner -- DrawMesh reads
+    the mesh's triangles on every call (context.go:435-439), so an edit
+    between draws is always drawn."""
+    from .meshops import DeviceMesh
+    if isinstance(mesh, DeviceMesh) or getattr(mesh, "resident", False):
+        return _upload_mesh(mesh), None
+    dm = DeviceMesh.upload(mesh)
+    return dm.handle, dm
+
+
 def _upload_texture(tex):
     lib = _abi.load_library()
     if tex._device is None:
@@ -170,18 +183,22 @@ class Context:
         return RasterizeInfo(int(info.total_pixels), int(info.updated_pixels))
 
     def DrawMesh(self, mesh):
-        """context.go:435-439."""
-        return self._info(self._lib.fgc_draw_mesh, _upload_mesh(mesh))
+        """context.go:435-439. A Mesh that is not resident (Mesh.MakeResident)
+        is uploaded for this draw from its current arrays."""
+        h, _owner = _draw_handle(mesh)
+        return self._info(self._lib.fgc_draw_mesh, h)
 
     def DrawTriangles(self, mesh, first=0, count=None):
         """context.go:413-433 over mesh triangles [first, first+count)."""
         count = mesh.ntri - first if count is None else count
-        return self._info(self._lib.fgc_draw_triangles, _upload_mesh(mesh), int(first), int(count))
+        h, _owner = _draw_handle(mesh)
+        return self._info(self._lib.fgc_draw_triangles, h, int(first), int(count))
 
     def DrawLines(self, mesh, first=0, count=None):
         """context.go:391-411 over mesh lines [first, first+count)."""
         count = mesh.nline - first if count is None else count
-        return self._info(self._lib.fgc_draw_lines, _upload_mesh(mesh), int(first), int(count))
+        h, _owner = _draw_handle(mesh)
+        return self._info(self._lib.fgc_draw_lines, h, int(first), int(count))
 
     def DrawTriangle(self, t):
         """context.go:370-389 for one Triangle object."""

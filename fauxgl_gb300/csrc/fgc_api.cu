@@ -408,6 +408,12 @@ int fgc_context_set_stream(fgc_context* c, void* cuda_stream) {
     return FGC_OK;
 }
 
+int fgc_debug_lookback(uint32_t spin_limit, uint32_t withhold_block) {
+    g_lookback_spin_limit.store(spin_limit ? spin_limit : kSpinLimit, std::memory_order_relaxed);
+    g_lookback_withhold.store(withhold_block, std::memory_order_relaxed);
+    return FGC_OK;
+}
+
 int fgc_measure_fp64_rate(double* gops_per_s) {
     if (!gops_per_s) return fail(FGC_ERR_INVALID_ARGUMENT, "null argument");
     int dev = 0, sms = 1;

@@ -416,6 +416,9 @@ __global__ void __launch_bounds__(kSetupTile) setup_kernel(GeomParams P) {
 // The FP64 half of setup: one thread per work item, every lane busy (the
 // work list holds only what survived culling), no barriers.
 __global__ void __launch_bounds__(256, 3) setup_emit_kernel(GeomParams P) {
+    // a look-back wait that gave up leaves the work list and its count
+    // inconsistent: emit nothing (the draw reports the failure)
+    if (*P.status & ST_LOOKBACK_TIMEOUT) return;
     if (blockIdx.x == 0)  // each draw's primitive range: setup_kernel wrote the starts and the total
         for (uint32_t i = threadIdx.x; i < P.nitems; i += blockDim.x)
             P.iout[i].prim_end = (i + 1 < P.nitems) ? P.iout[i + 1].prim_start : *P.prim_total;

@@ -9,6 +9,8 @@
 // batch interface runs passes of many draws asynchronously.
 #pragma once
 
+#include <atomic>
+
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -87,6 +89,19 @@ struct PinnedBuf {
 };
 
 constexpr int kRasterThreads = 256;
+
+// The look-back of the draw pipeline's ordered allocations and scans: the
+// limit on polls of an unpublished predecessor (kSpinLimit) and no withheld
+// block, unless fgc_debug_lookback set a test configuration.
+extern std::atomic<uint32_t> g_lookback_spin_limit;
+extern std::atomic<uint32_t> g_lookback_withhold;
+inline Lookback draw_lookback(unsigned long long* tiles, unsigned int* ticket, unsigned int* status,
+                              unsigned long long* total) {
+    Lookback L{tiles, ticket, status, total};
+    L.spin_limit = g_lookback_spin_limit.load(std::memory_order_relaxed);
+    L.withhold = g_lookback_withhold.load(std::memory_order_relaxed);
+    return L;
+}
 constexpr int kMaxBands = 24576;
 
 uint32_t pack_nrgba_host(const double c[4]);

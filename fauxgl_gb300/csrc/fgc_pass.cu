@@ -22,6 +22,9 @@
 
 namespace fgc {
 
+std::atomic<uint32_t> g_lookback_spin_limit{kSpinLimit};
+std::atomic<uint32_t> g_lookback_withhold{0xFFFFFFFFu};
+
 namespace {
 
 constexpr size_t kHeaderBytes = 80;
@@ -462,7 +465,7 @@ int issue_submission(PassScratch& S, cudaStream_t stream, const DevLimits& D, co
         gp.pool = S.pool.p;
         gp.pool32 = S.pool32.p;
         gp.prim_total = &dc->prim_total;
-        gp.lb = Lookback{t_setup, &dc->tick_setup, status, nullptr};  // setup_kernel writes the totals
+        gp.lb = draw_lookback(t_setup, &dc->tick_setup, status, nullptr);  // setup_kernel writes the totals
         gp.status = status;
         gp.work = S.work.p;
         gp.work_cap = S.work.cap;
@@ -520,7 +523,7 @@ int issue_submission(PassScratch& S, cudaStream_t stream, const DevLimits& D, co
         sp.in = S.mat.p;
         sp.out = S.off.p;
         sp.n = P.nmat;
-        sp.lb = Lookback{t_scan, &dc->tick_scan, status, &dc->pair_total};
+        sp.lb = draw_lookback(t_scan, &dc->tick_scan, status, &dc->pair_total);
         scan_u32_kernel<<<P.scan_tiles, 256, 0, stream>>>(sp);
         FGC_CUDA(cudaGetLastError());
         const size_t scat_smem = (size_t)P.bin_warps * P.max_nbands * 4;
@@ -535,7 +538,7 @@ int issue_submission(PassScratch& S, cudaStream_t stream, const DevLimits& D, co
             rsp.in = S.pnb.p;
             rsp.out = S.prs.p;
             rsp.n = prim_cap0;
-            rsp.lb = Lookback{t_rscan, &dc->tick_rscan, status, &dc->reserved};
+            rsp.lb = draw_lookback(t_rscan, &dc->tick_rscan, status, &dc->reserved);
             rsp.n_dev = &dc->prim_total;  // bin_count wrote the band counts of these
             scan_u32_kernel<<<(unsigned)rs_tiles, 256, 0, stream>>>(rsp);
             FGC_CUDA(cudaGetLastError());

@@ -6,8 +6,8 @@
 // earlier elements, so records land in submission order with one pass over
 // the input. Logical block indices come from an atomic ticket so every
 // predecessor of a block has already started; each wait on a predecessor is
-// bounded (kSpinLimit polls) and reports ST_LOOKBACK_TIMEOUT instead of
-// hanging.
+// bounded (kSpinLimit polls unless the host sets a smaller limit) and
+// reports ST_LOOKBACK_TIMEOUT instead of hanging.
 #pragma once
 
 #include "fgc_device.cuh"
@@ -23,6 +23,8 @@ struct Lookback {
     unsigned int* ticket;       // zeroed before launch
     unsigned int* status;       // device status word
     unsigned long long* total;  // receives the grand total (written by the last block)
+    uint32_t spin_limit = kSpinLimit;   // polls of an unpublished predecessor before giving up
+    uint32_t withhold = 0xFFFFFFFFu;    // test hook: this logical block never publishes
 };
 
 template <int BLOCK>
@@ -76,10 +78,11 @@ __device__ __forceinline__ uint64_t lookback_prefix(const Lookback& L, uint32_t 
     if (threadIdx.x < 32) {
         const uint32_t lane = threadIdx.x;
         uint64_t excl = 0;
+        const bool publish = tile != L.withhold;
         if (tile == 0) {
-            if (lane == 0) atomicExch(&L.tiles[0], (unsigned long long)(kFlagPre | (agg & kValMask)));
+            if (lane == 0 && publish) atomicExch(&L.tiles[0], (unsigned long long)(kFlagPre | (agg & kValMask)));
         } else {
-            if (lane == 0) atomicExch(&L.tiles[tile], (unsigned long long)(kFlagAgg | (agg & kValMask)));
+            if (lane == 0 && publish) atomicExch(&L.tiles[tile], (unsigned long long)(kFlagAgg | (agg & kValMask)));
             int64_t hi = (int64_t)tile - 1;  // the window is tiles hi, hi-1, ..., hi-31 (lane order)
             uint32_t spins = 0;
             for (;;) {
@@ -92,7 +95,7 @@ __device__ __forceinline__ uint64_t lookback_prefix(const Lookback& L, uint32_t 
                 // lanes up to the nearest inclusive prefix (all 32 when there is none)
                 const uint32_t upto = pre ? ((pre & (0u - pre)) << 1) - 1u : 0xffffffffu;
                 if (unset & upto) {
-                    if (++spins > kSpinLimit) {
+                    if (++spins > L.spin_limit) {
                         if (lane == 0) atomicOr(L.status, ST_LOOKBACK_TIMEOUT);
                         break;
                     }
@@ -106,7 +109,8 @@ __device__ __forceinline__ uint64_t lookback_prefix(const Lookback& L, uint32_t 
                 if (pre) break;
                 hi -= 32;
             }
-            if (lane == 0) atomicExch(&L.tiles[tile], (unsigned long long)(kFlagPre | ((excl + agg) & kValMask)));
+            if (lane == 0 && publish)
+                atomicExch(&L.tiles[tile], (unsigned long long)(kFlagPre | ((excl + agg) & kValMask)));
         }
         if (lane == 0) {
             if (tile == gridDim.x - 1 && L.total) *L.total = excl + agg;

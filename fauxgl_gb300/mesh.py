@@ -165,6 +165,7 @@ class Mesh:
         self.line_col = arr(line_col, (2, 4))
         self._device = None
         self._device_key = None
+        self.resident = False
 
     # -- sizes ------------------------------------------------------------
     @property
@@ -179,6 +180,16 @@ class Mesh:
         """Forget the device copy after the arrays were changed in place."""
         self._device = None
         self._device_key = None
+
+    def MakeResident(self):
+        """Keep a device copy of this mesh between draws (no counterpart in
+        package fauxgl, whose DrawMesh reads mesh.Triangles on every call).
+        A draw of a mesh that is not resident uploads it for that draw only,
+        so edits between draws are always seen; a resident mesh is uploaded
+        once, and the methods here that change it drop the copy themselves,
+        but an edit of its arrays in place must be followed by dirty()."""
+        self.resident = True
+        return self
 
     # -- construction from reference-style objects -------------------------
     @staticmethod

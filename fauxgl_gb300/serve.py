@@ -14,7 +14,12 @@ A Server keeps a pool of meshes resident on the GPU and renders requests --
     start as slots and memory free up and their work overlaps on the device;
   * results: each request's frame is cleared, drawn, box-downsampled by its
     scale on the device and copied to the host; its latency runs from arrival
-    to that copy's completion.
+    to that copy's completion;
+  * deadlines and cancellation: a request still waiting for admission
+    request_timeout seconds after its arrival expires (load shedding when the
+    offered rate is above what the GPU sustains), and cancel() withdraws a
+    waiting request at once or discards a running one's result when its
+    batch finishes (work on the GPU is never interrupted).
 
 Each request's result does not depend on what it is batched with: every draw
 of a batch gives exactly what it gives alone (same kernels, same per-draw
@@ -53,22 +58,28 @@ class Request:
     background: tuple = (1.0, 1.0, 1.0, 1.0)
 
 
-@dataclass
+@dataclass(eq=False)  # tickets are compared by identity (two requests may be alike)
 class Ticket:
     request: Request
     arrival: float
     admitted: float = 0.0
     finished: float = 0.0
-    done: bool = False
+    done: bool = False             # the result is ready
+    status: str = "pending"        # pending, running, done, cancelled or expired
     image: np.ndarray = None
     info: tuple = None
     bytes: int = 0
     scratch: int = 0
+    cancel_requested: bool = False
     _ctx: object = field(default=None, repr=False)
 
     @property
     def latency_s(self):
         return self.finished - self.arrival if self.done else None
+
+    @property
+    def dropped(self):
+        return self.status in ("cancelled", "expired")
 
 
 def _pinned(nbytes):
@@ -107,7 +118,8 @@ class Server:
     """Continuous-batching render server over a resident mesh pool."""
 
     def __init__(self, meshes, hbm_budget=32 << 30, slots=3, max_batch=64, precision=_abi.FGC_PRECISION_MIXED,
-                 tuning=None, lib=None, upload=None):
+                 tuning=None, lib=None, upload=None, request_timeout=None, clock=time.perf_counter,
+                 max_batch_triangles=16 << 20):
         # lib / upload stand in for libfauxglcuda and the mesh upload in the
         # host-logic tests
         self.lib = lib or _abi.load_library()
@@ -115,13 +127,17 @@ class Server:
         self.mesh_handles = [(upload or _upload_mesh)(m) for m in self.meshes]
         self.budget = int(hbm_budget)
         self.max_batch = int(max_batch)
+        self.max_batch_triangles = int(max_batch_triangles)  # a batch's scratch grows with its triangles
         self.precision = precision
         self.slots = [_Slot(self.lib) for _ in range(max(1, slots))]
         if tuning:
             t = _abi.FgcBatchTuning(*tuning)
             for s in self.slots:
                 _abi.check(self.lib.fgc_batch_set_tuning(s.h.handle, ctypes.byref(t)))
+        self.request_timeout = request_timeout  # seconds a request may wait for admission (None: forever)
+        self.clock = clock
         self.pending = deque()
+        self.dropped = []    # cancelled and expired tickets
         self.contexts = {}   # (W, H) -> [idle contexts], kept for reuse
         self.fb_bytes = 0    # framebuffers of every live context (idle or in use)
         self.scratch = 0     # scratch share of the requests on the GPU
@@ -138,7 +154,7 @@ class Server:
                 + SCRATCH_BYTES_PER_TRIANGLE * self.meshes[r.mesh].ntri)
 
     def submit(self, request, arrival=None):
-        t = Ticket(request, time.perf_counter() if arrival is None else arrival)
+        t = Ticket(request, self.clock() if arrival is None else arrival)
         t.bytes = self.request_bytes(request)
         if t.bytes > self.budget:
             raise ValueError("request needs %d bytes, above the HBM budget %d" % (t.bytes, self.budget))
@@ -148,6 +164,32 @@ class Server:
     @property
     def in_use(self):
         return self.fb_bytes + self.scratch
+
+    def cancel(self, ticket):
+        """Withdraw a request: a waiting one leaves the queue now; a running
+        one's result is discarded when its batch finishes. Returns False when
+        the result was already delivered (or the ticket already dropped)."""
+        if ticket.status == "pending":
+            self.pending.remove(ticket)
+            self._drop(ticket, "cancelled")
+            return True
+        if ticket.status == "running":
+            ticket.cancel_requested = True
+            return True
+        return False
+
+    def _drop(self, t, status):
+        t.status = status
+        t.finished = self.clock()
+        self.dropped.append(t)
+
+    def _expire(self, now):
+        """Requests that waited for admission longer than request_timeout."""
+        if self.request_timeout is None:
+            return
+        # the queue is in arrival order: the oldest waiting requests lead it
+        while self.pending and now - self.pending[0].arrival > self.request_timeout:
+            self._drop(self.pending.popleft(), "expired")
 
     # -- contexts ---------------------------------------------------------------
     def _fits(self, t):
@@ -189,10 +231,10 @@ class Server:
         """Finish the batches that are done, then admit pending requests into
         free slots. Returns the tickets finished by this call."""
         finished = []
-        now = time.perf_counter()
         for s in self.slots:
             if s.busy and s.done():
                 finished += self._finish(s)
+        self._expire(self.clock())
         for s in self.slots:
             if not self.pending:
                 break
@@ -207,10 +249,15 @@ class Server:
 
     def _admit(self, slot):
         batch, ctxs = [], []
+        tris = 0
         while self.pending and len(batch) < self.max_batch:
             t = self.pending[0]
+            ntri = self.meshes[t.request.mesh].ntri
+            if batch and tris + ntri > self.max_batch_triangles:
+                break
             if not self._fits(t):
                 break
+            tris += ntri
             self.pending.popleft()
             r = t.request
             ctxs.append(self._context(r.width * r.scale, r.height * r.scale))
@@ -222,12 +269,13 @@ class Server:
         n = len(batch)
         items = (_abi.FgcBatchItem * n)()
         keep = [items]
-        now = time.perf_counter()
+        now = self.clock()
         for i, t in enumerate(batch):
             r = t.request
             ctx = ctxs[i]
             t._ctx = ctx
             t.admitted = now
+            t.status = "running"
             c = (ctypes.c_double * 4)(*r.background)
             _abi.check(self.lib.fgc_clear_color(ctx.handle, c))
             _abi.check(self.lib.fgc_clear_depth(ctx.handle, 1.7976931348623157e308))
@@ -259,16 +307,21 @@ class Server:
         n = len(slot.tickets)
         infos = (_abi.FgcRasterizeInfo * n)()
         _abi.check(self.lib.fgc_batch_wait(slot.h.handle, infos))
-        now = time.perf_counter()
+        now = self.clock()
         out = []
         for i, t in enumerate(slot.tickets):
             r = t.request
-            t.info = (int(infos[i].total_pixels), int(infos[i].updated_pixels))
-            t.finished = now
-            t.done = True
             self._release(r.width * r.scale, r.height * r.scale, t._ctx)
             t._ctx = None
             self.scratch -= t.scratch
+            if t.cancel_requested:
+                t.image = None
+                self._drop(t, "cancelled")
+                continue
+            t.info = (int(infos[i].total_pixels), int(infos[i].updated_pixels))
+            t.finished = now
+            t.done = True
+            t.status = "done"
             out.append(t)
         self.completed += out
         slot.tickets = []
@@ -313,30 +366,39 @@ def poisson_arrivals(rate, duration, seed):
         out.append(t)
 
 
-def run_load(server, requests, arrivals, timeout=None):
+def run_load(server, requests, arrivals, timeout=None, sleep=time.sleep):
     """Drive the server with requests arriving at the given times (seconds
-    from start); returns the finished tickets in completion order."""
-    start = time.perf_counter()
+    from start); returns (tickets in arrival order, elapsed seconds). With a
+    timeout (seconds), requests not finished by then are cancelled: arrivals
+    after it are never submitted, waiting ones leave the queue and running
+    batches are finished with their results discarded, so the server is idle
+    and reusable on return."""
+    clock = server.clock
+    start = clock()
     tickets = []
     i = 0
     deadline = None if timeout is None else start + timeout
     while i < len(requests) or server.pending or any(s.busy for s in server.slots):
-        now = time.perf_counter()
+        now = clock()
+        if deadline is not None and now > deadline:
+            for t in list(server.pending) + [t for s in server.slots for t in s.tickets]:
+                server.cancel(t)
+            server.drain()
+            break
         while i < len(requests) and now - start >= arrivals[i]:
             tickets.append(server.submit(requests[i], arrival=start + arrivals[i]))
             i += 1
         server.poll()
-        if deadline is not None and now > deadline:
-            break
         if i < len(requests) and not server.pending and not any(s.busy for s in server.slots):
             # idle until the next arrival
-            wait = start + arrivals[i] - time.perf_counter()
+            wait = start + arrivals[i] - clock()
             if wait > 0:
-                time.sleep(min(wait, 0.002))
-    return tickets, time.perf_counter() - start
+                sleep(min(wait, 0.002))
+    return tickets, clock() - start
 
 
 def latency_summary(tickets):
+    """p50 / p99 latency of the delivered results (dropped requests excluded)."""
     lat = sorted(t.latency_s for t in tickets if t.done)
     if not lat:
         return {"p50_ms": None, "p99_ms": None, "n": 0}

@@ -273,6 +273,16 @@ int fgc_context_last_stats(const fgc_context* ctx, fgc_stats* out);
 /* Run the context's work on a caller-owned cudaStream_t (NULL restores the
  * context's own stream). */
 int fgc_context_set_stream(fgc_context* ctx, void* cuda_stream);
+/* Test hook for the failure path of the draw pipeline's bounded waits (no
+ * reference counterpart). The setup and scan stages allocate in submission
+ * order by a decoupled look-back in which each block waits, a bounded number
+ * of polls, for its predecessors to publish their counts; a wait that runs
+ * out makes the draw return FGC_ERR_DEVICE_LIMIT with its framebuffers
+ * untouched. spin_limit sets that number of polls (0: the default,
+ * 2^22) and withhold_block names a logical block that never publishes
+ * (0xFFFFFFFF: none), so a test can make the waits run out on purpose; the
+ * setting is process-wide and applies to draws issued after the call. */
+int fgc_debug_lookback(uint32_t spin_limit, uint32_t withhold_block);
 /* FP64 pipe throughput of the current device, measured: independent FP64
  * adds issued on every SM, in G instructions per second. It is the roofline
  * denominator of the FP64-bound stages (one add, multiply or compare is one

@@ -175,3 +175,92 @@ def test_poisson_arrivals_and_summary():
     assert all(0 <= x < 2.0 for x in a) and a == sorted(a)
     assert 300 < len(a) < 500
     assert latency_summary([]) == {"p50_ms": None, "p99_ms": None, "n": 0}
+
+
+class FakeClock:
+    """A clock the test moves by hand (and run_load's sleep moves too)."""
+
+    def __init__(self):
+        self.t = 0.0
+
+    def __call__(self):
+        return self.t
+
+    def sleep(self, dt):
+        self.t += dt
+
+
+def make_timed_server(budget=1 << 40, slots=1, max_batch=2, latency=3, request_timeout=None):
+    lib = FakeLib(latency)
+    clock = FakeClock()
+    srv = Server([FakeMesh(1000)], hbm_budget=budget, slots=slots, max_batch=max_batch, lib=lib,
+                 upload=lambda m: id(m), request_timeout=request_timeout, clock=clock)
+    return srv, lib, clock
+
+
+def test_cancel_waiting_and_running_requests():
+    srv, lib, clock = make_timed_server(slots=1, max_batch=2, latency=3)
+    ts = [srv.submit(req()) for _ in range(5)]
+    srv.poll()  # the first two run, three wait
+    assert [t.status for t in ts] == ["running", "running", "pending", "pending", "pending"]
+    assert srv.cancel(ts[3])            # waiting: leaves the queue at once
+    assert ts[3].status == "cancelled" and ts[3] not in srv.pending
+    assert srv.cancel(ts[1])            # running: the batch finishes, its result is dropped
+    assert ts[1].status == "running" and ts[1].cancel_requested
+    srv.drain()
+    assert [t.status for t in ts] == ["done", "cancelled", "done", "cancelled", "done"]
+    assert ts[1].image is None and not ts[1].done and ts[1].latency_s is None
+    assert not srv.cancel(ts[0])        # delivered results cannot be withdrawn
+    assert len(lib.submissions) == 2    # the cancelled waiting request never reached the GPU
+    assert srv.scratch == 0             # every admitted request released its share
+    assert latency_summary(ts)["n"] == 3
+    assert {id(t) for t in srv.dropped} == {id(ts[1]), id(ts[3])}
+
+
+def test_waiting_requests_expire_after_the_request_timeout():
+    srv, lib, clock = make_timed_server(slots=1, max_batch=1, latency=2, request_timeout=0.5)
+    ts = [srv.submit(req()) for _ in range(4)]
+    srv.poll()                # one runs, three wait
+    clock.t = 0.4
+    srv.poll()                # the first finishes after two queries; the second is admitted
+    srv.poll()
+    clock.t = 0.6             # the two still waiting are now past the timeout
+    srv.drain()
+    assert [t.status for t in ts] == ["done", "done", "expired", "expired"]
+    assert len(lib.submissions) == 2
+    assert all(t.finished == 0.6 for t in ts[2:])
+
+
+def test_run_load_timeout_cancels_unfinished_work():
+    from fauxgl_gb300.serve import run_load
+    srv, lib, clock = make_timed_server(slots=1, max_batch=1, latency=1000000)  # batches never finish by themselves
+    reqs = [req() for _ in range(4)]
+    lib.latency = 4
+    arrivals = [0.0, 0.0, 0.01, 10.0]       # the last arrives after the deadline
+    orig_poll = srv.poll
+
+    def slow_poll():                        # each poll takes 5 ms of the fake clock
+        clock.t += 0.005
+        return orig_poll()
+    srv.poll = slow_poll
+    tickets, elapsed = run_load(srv, reqs, arrivals, timeout=0.012, sleep=clock.sleep)
+    assert len(tickets) == 3                # the fourth was never submitted
+    assert tickets[0].status in ("done", "cancelled")
+    assert all(t.status in ("done", "cancelled") for t in tickets)
+    assert any(t.status == "cancelled" for t in tickets)
+    assert not srv.pending and not any(s.busy for s in srv.slots)  # idle and reusable
+    assert srv.scratch == 0
+    t = srv.submit(req())
+    srv.drain()
+    assert t.status == "done"
+
+
+def test_batches_stop_at_their_triangle_cap():
+    lib = FakeLib(2)
+    srv = Server([FakeMesh(1000), FakeMesh(2000)], hbm_budget=1 << 40, slots=1, max_batch=8, lib=lib,
+                 upload=lambda m: id(m), max_batch_triangles=3500)
+    ts = [srv.submit(req(mesh=m)) for m in (0, 1, 0, 1, 1)]
+    srv.drain()
+    assert all(t.done for t in ts)
+    # 1000 + 2000 fit, the next 1000 would pass 3500; a lone request always runs
+    assert [len(s) for s in lib.submissions] == [2, 2, 1]
