@@ -358,66 +358,156 @@ __device__ __forceinline__ SetupElem classify(const GeomParams& P, const ItemVie
     return e;
 }
 
-// kSetupPer consecutive elements per thread, so that the slots and work
-// items of a thread's elements follow one another.
-__global__ void __launch_bounds__(kSetupTile) setup_kernel(GeomParams P) {
-    __shared__ uint32_t s_tile;
-    __shared__ OrderedAllocSmem<kSetupTile> s_alloc;
-    const uint32_t tile = block_ticket<kSetupTile>(P.lb, &s_tile);
-    const uint32_t item = find_item(P.starts.stile, P.nitems, tile);
-    const ItemView& I = P.items[item];
-    const uint32_t lt = tile - I.stile0;
-    const bool tri = lt < I.ntri_tiles;
-    const uint64_t k0 = (uint64_t)(tri ? lt : lt - I.ntri_tiles) * (kSetupTile * kSetupPer) +
-                        (uint64_t)kSetupPer * threadIdx.x;
-    const uint8_t* vout = P.vout + I.vbase;
+// The setup decision of an element in 16 bits: primitive slots (6 bits: 0,
+// 1, 2, 6, 7 or 42), work items (2 bits), cull order + 1 (2 bits), clip.
+__device__ __forceinline__ uint16_t pack_meta(const SetupElem& e) {
+    return (uint16_t)(e.count | (e.work << 6) | ((uint32_t)(e.order + 1) << 8) | ((e.clip ? 1u : 0u) << 10));
+}
 
-    SetupElem el[kSetupPer];
+// A setup tile: its draw, its index within the draw and its first element
+// for this thread (kSetupPer consecutive elements per thread, so that the
+// slots and work items of a thread's elements follow one another).
+struct SetupTileOf {
+    uint32_t item, lt;
+    bool tri;
+    uint64_t k0;
+};
+__device__ __forceinline__ SetupTileOf setup_tile_of(const GeomParams& P, uint32_t tile) {
+    SetupTileOf T;
+    T.item = find_item(P.starts.stile, P.nitems, tile);
+    const ItemView& I = P.items[T.item];
+    T.lt = tile - I.stile0;
+    T.tri = T.lt < I.ntri_tiles;
+    T.k0 = (uint64_t)(T.tri ? T.lt : T.lt - I.ntri_tiles) * (kSetupTile * kSetupPer) + (uint64_t)kSetupPer * threadIdx.x;
+    return T;
+}
+
+// Setup in three launches, none of which waits on another block: the count
+// kernel decides every element (culling, clipping, slots, work items) and
+// sums each tile; one block scans the tile sums; the list kernel gives every
+// element its slots and work-list positions from its tile's prefix and the
+// block scan of the decisions.
+__global__ void __launch_bounds__(kSetupTile) setup_count_kernel(GeomParams P) {
+    __shared__ uint64_t s_warp[kSetupTile / 32 + 1];
+    const uint32_t tile = blockIdx.x;
+    const SetupTileOf T = setup_tile_of(P, tile);
+    const ItemView& I = P.items[T.item];
+    const uint8_t* vout = P.vout + I.vbase;
+    uint16_t* meta = P.smeta + (uint64_t)tile * (kSetupTile * kSetupPer) + (uint64_t)kSetupPer * threadIdx.x;
     uint32_t count = 0, work = 0;
 #pragma unroll
     for (int j = 0; j < kSetupPer; j++) {
-        el[j] = classify(P, I, tri, k0 + j, vout);
-        count += el[j].count;
-        work += el[j].work;
+        const SetupElem e = classify(P, I, T.tri, T.k0 + j, vout);
+        meta[j] = pack_meta(e);
+        count += e.count;
+        work += e.work;
     }
-    uint64_t slot, wpos, total;
-    ordered_alloc2<kSetupTile>(P.lb, tile, count, work, s_alloc, slot, wpos, total);
-    if (lt == 0 && threadIdx.x == 0) P.iout[item].prim_start = slot;  // thread 0's local prefix is 0
-    if (tile == gridDim.x - 1 && threadIdx.x == 0) {
-        *P.prim_total = total >> 31;
-        *P.work_total = total & kLow31;
+    uint64_t agg;
+    block_exclusive_scan<kSetupTile>(((uint64_t)count << 31) | work, s_warp, &agg);
+    if (threadIdx.x == 0) P.tsum[tile] = agg;
+}
+
+// Exclusive scan of the tile sums in place, one block; the slot and work
+// totals of the pass. Both fields of the packed sums stay below 2^31 (the
+// host keeps a pass's slots and work items below it), so they add without
+// carries into each other.
+constexpr int kSetupScanThreads = 1024;
+__global__ void __launch_bounds__(kSetupScanThreads) setup_scan_kernel(GeomParams P) {
+    __shared__ uint64_t s_warp[kSetupScanThreads / 32 + 1];
+    __shared__ uint64_t s_carry;
+    constexpr int kPer = 4;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    for (uint64_t base = 0; base < P.ntiles; base += (uint64_t)kSetupScanThreads * kPer) {
+        const uint64_t i0 = base + (uint64_t)threadIdx.x * kPer;
+        uint64_t v[kPer], sum = 0;
+#pragma unroll
+        for (int j = 0; j < kPer; j++) {
+            v[j] = (i0 + j < P.ntiles) ? P.tsum[i0 + j] : 0ull;
+            sum += v[j];
+        }
+        uint64_t agg;
+        uint64_t run = block_exclusive_scan<kSetupScanThreads>(sum, s_warp, &agg) + s_carry;
+#pragma unroll
+        for (int j = 0; j < kPer; j++) {
+            if (i0 + j < P.ntiles) P.tsum[i0 + j] = run;
+            run += v[j];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry += agg;
+        __syncthreads();
     }
+    if (threadIdx.x == 0) {
+        *P.prim_total = s_carry >> 31;
+        *P.work_total = s_carry & kLow31;
+    }
+}
+
+__global__ void __launch_bounds__(kSetupTile) setup_kernel(GeomParams P) {
+    __shared__ uint64_t s_warp[kSetupTile / 32 + 1];
+    const uint32_t tile = blockIdx.x;
+    const SetupTileOf T = setup_tile_of(P, tile);
+    const ItemView& I = P.items[T.item];
+    const bool tri = T.tri;
+    const uint16_t* meta = P.smeta + (uint64_t)tile * (kSetupTile * kSetupPer) + (uint64_t)kSetupPer * threadIdx.x;
+    uint16_t m[kSetupPer];
+    uint32_t count = 0, work = 0;
 #pragma unroll
     for (int j = 0; j < kSetupPer; j++) {
-        const SetupElem& e = el[j];
-        const uint64_t k = k0 + j;
-        if (e.count != 0 && e.clip) {
+        m[j] = meta[j];
+        count += m[j] & 63u;
+        work += (m[j] >> 6) & 3u;
+    }
+    uint64_t agg;
+    const uint64_t local = block_exclusive_scan<kSetupTile>(((uint64_t)count << 31) | work, s_warp, &agg);
+    const uint64_t base = P.tsum[tile];
+    uint64_t slot = (base >> 31) + (local >> 31);
+    uint64_t wpos = (base & kLow31) + (local & kLow31);
+    if (T.lt == 0 && threadIdx.x == 0) P.iout[T.item].prim_start = slot;  // thread 0's local prefix is 0
+#pragma unroll
+    for (int j = 0; j < kSetupPer; j++) {
+        const uint32_t ecount = m[j] & 63u, ework = (m[j] >> 6) & 3u;
+        const bool eclip = (m[j] >> 10) & 1u;
+        const uint64_t k = T.k0 + j;
+        if (ecount != 0 && eclip) {
             if (tri) {
-                append_clip(P, item, I.tri_first + k, slot);
+                append_clip(P, T.item, I.tri_first + k, slot);
             } else {
                 uint32_t idx = atomicAdd(P.lclip_count, 1u);
-                P.lclip_list[idx] = ClipEntry{slot, (uint32_t)(I.line_first + k), item};  // holds every line of the pass
+                P.lclip_list[idx] = ClipEntry{slot, (uint32_t)(I.line_first + k), T.item};  // holds every line of the pass
             }
         }
-        const uint32_t elem = (uint32_t)((tri ? I.tri_first : I.line_first) + k);
-        const uint32_t meta = (uint32_t)(e.order + 1) << 8 | (tri ? 0u : kWorkLine);
-        for (uint32_t w = 0; w < e.work; w++) {
-            if (wpos + w >= P.work_cap) {  // sized for every element: not reached
-                atomicOr(P.status, ST_RASTER_INTERNAL);
-                break;
+        if (ework) {
+            const uint32_t elem = (uint32_t)((tri ? I.tri_first : I.line_first) + k);
+            const uint32_t meta8 = ((m[j] >> 8) & 3u) << 8 | (tri ? 0u : kWorkLine);
+            uint32_t u0, u1, u2 = 0;
+            if (tri) {
+                u0 = I.mesh.corner_uniq[3 * (uint64_t)elem + 0];
+                u1 = I.mesh.corner_uniq[3 * (uint64_t)elem + 1];
+                u2 = I.mesh.corner_uniq[3 * (uint64_t)elem + 2];
+            } else {
+                const uint64_t cb = 3 * I.mesh.ntri + 2 * (uint64_t)elem;
+                u0 = I.mesh.corner_uniq[cb];
+                u1 = I.mesh.corner_uniq[cb + 1];
             }
-            P.work[wpos + w] = SetupWork{slot, elem, item, e.u0, e.u1, e.u2, meta | w};
+            for (uint32_t w = 0; w < ework; w++) {
+                if (wpos + w >= P.work_cap) {  // sized for every element: not reached
+                    atomicOr(P.status, ST_RASTER_INTERNAL);
+                    break;
+                }
+                P.work[wpos + w] = SetupWork{slot, elem, T.item, u0, u1, u2, meta8 | w};
+            }
         }
-        slot += e.count;
-        wpos += e.work;
+        slot += ecount;
+        wpos += ework;
     }
 }
 
 // The FP64 half of setup: one thread per work item, every lane busy (the
 // work list holds only what survived culling), no barriers.
 __global__ void __launch_bounds__(256, 3) setup_emit_kernel(GeomParams P) {
-    // a look-back wait that gave up leaves the work list and its count
-    // inconsistent: emit nothing (the draw reports the failure)
+    // a look-back wait that gave up (a scan of an earlier pass) leaves the
+    // pass to be reported as failed: emit nothing
     if (*P.status & ST_LOOKBACK_TIMEOUT) return;
     if (blockIdx.x == 0)  // each draw's primitive range: setup_kernel wrote the starts and the total
         for (uint32_t i = threadIdx.x; i < P.nitems; i += blockDim.x)

@@ -222,6 +222,8 @@ struct PassScratch {
     DevBuf<unsigned char> table;   // item views + lookup starts + per-draw results + counters + status
     DevBuf<double> dbg;
     DevBuf<SetupWork> work;        // setup work items (triangles, wireframe edges, lines)
+    DevBuf<uint16_t> smeta;        // per element of a setup tile: its setup decision
+    DevBuf<unsigned long long> tsum;  // per setup tile: its sums, then their exclusive prefix
     PinnedBuf host_in, host_out;
     uint32_t clip_cap = 1024;
     uint64_t bin_cap = 0;

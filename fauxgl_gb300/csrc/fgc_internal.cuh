@@ -136,6 +136,8 @@ struct GeomParams {
     SetupWork* work;            // the primitive-emitting work items, in slot order
     uint64_t work_cap;
     unsigned long long* work_total;
+    uint16_t* smeta;            // per element of a setup tile: its setup decision (setup_count -> setup_kernel)
+    unsigned long long* tsum;   // per setup tile: slots << 31 | work items, then their exclusive prefix
 };
 constexpr int kSetupTile = 256;  // threads of a setup tile
 constexpr int kSetupPer = 2;     // consecutive elements per thread
@@ -237,6 +239,8 @@ struct RasterParams {
 
 // Kernels (grid shapes chosen by the host runtime).
 __global__ void vertex_kernel(VertexParams P);
+__global__ void setup_count_kernel(GeomParams P);
+__global__ void setup_scan_kernel(GeomParams P);
 __global__ void setup_kernel(GeomParams P);
 __global__ void setup_emit_kernel(GeomParams P);
 __global__ void clip_triangles_kernel(GeomParams P);

@@ -325,6 +325,10 @@ int plan_submission(PassScratch& S, const DevLimits& D, const PassTuning& T, con
     FGC_CUDA(S.rstart.ensure(3 * S.bin_cap));
     FGC_CUDA(S.tiles.ensure(need_tiles));
     FGC_CUDA(S.work.ensure(need_work));
+    uint64_t need_stiles = 1;
+    for (const PassPlan& P : plans) need_stiles = std::max<uint64_t>(need_stiles, P.stiles);
+    FGC_CUDA(S.smeta.ensure(need_stiles * kSetupTile * kSetupPer));
+    FGC_CUDA(S.tsum.ensure(need_stiles));
     FGC_CUDA(S.table.ensure(TL.total));
     int dev = 0;
     FGC_CUDA(cudaGetDevice(&dev));
@@ -470,9 +474,13 @@ int issue_submission(PassScratch& S, cudaStream_t stream, const DevLimits& D, co
         gp.work = S.work.p;
         gp.work_cap = S.work.cap;
         gp.work_total = &dc->work_total;
+        gp.smeta = S.smeta.p;
+        gp.tsum = S.tsum.p;
+        setup_count_kernel<<<P.stiles, kSetupTile, 0, stream>>>(gp);
+        setup_scan_kernel<<<1, 1024, 0, stream>>>(gp);
         setup_kernel<<<P.stiles, kSetupTile, 0, stream>>>(gp);
         FGC_CUDA(cudaGetLastError());
-        rec.launches++;
+        rec.launches += 3;
         // the clip kernels (latency-bound: one long FP64 chain per entry) run
         // on the side stream while the emission fills every SM's FP64 pipe
         const bool clips = P.any_tri || P.any_line;
@@ -617,7 +625,7 @@ int collect_submission(PassScratch& S, Submission& sub, size_t from, size_t* ret
         if (h->status & ST_RASTER_INTERNAL)
             return fail(FGC_ERR_DEVICE_LIMIT, "the raster stage detected an internal inconsistency");
         if (h->status & ST_LOOKBACK_TIMEOUT)
-            return fail(FGC_ERR_DEVICE_LIMIT, "a look-back wait in the setup or scan stage timed out");
+            return fail(FGC_ERR_DEVICE_LIMIT, "a look-back wait in a scan of the binning stage timed out");
         if ((h->status & overflow) && first_bad == sub.passes.size()) first_bad = g;
         if (first_bad <= g) {
             clip_need = std::max(clip_need, h->c.clip_count);

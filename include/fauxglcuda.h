@@ -274,11 +274,11 @@ int fgc_context_last_stats(const fgc_context* ctx, fgc_stats* out);
  * context's own stream). */
 int fgc_context_set_stream(fgc_context* ctx, void* cuda_stream);
 /* Test hook for the failure path of the draw pipeline's bounded waits (no
- * reference counterpart). The setup and scan stages allocate in submission
- * order by a decoupled look-back in which each block waits, a bounded number
- * of polls, for its predecessors to publish their counts; a wait that runs
- * out makes the draw return FGC_ERR_DEVICE_LIMIT with its framebuffers
- * untouched. spin_limit sets that number of polls (0: the default,
+ * reference counterpart). The binning stage's scans (bin offsets, row-start
+ * slots) run in one pass by a decoupled look-back in which each block waits,
+ * a bounded number of polls, for its predecessors to publish their sums; a
+ * wait that runs out makes the draw return FGC_ERR_DEVICE_LIMIT with its
+ * framebuffers untouched. spin_limit sets that number of polls (0: the default,
  * 2^22) and withhold_block names a logical block that never publishes
  * (0xFFFFFFFF: none), so a test can make the waits run out on purpose; the
  * setting is process-wide and applies to draws issued after the call. */

@@ -1,10 +1,10 @@
 """GPU failure path of the bounded waits, without a GPU fault.
 
-The setup stage allocates raster primitives in submission order by a
-decoupled look-back: each block of triangles waits, for a bounded number of
-polls, until its predecessors have published their counts. The test hook
-fgc_debug_lookback shortens that bound and names a block that never
-publishes, so the waits of the blocks after it run out. The draw must then
+The binning stage scans its bin counts in one pass by a decoupled
+look-back: each block waits, for a bounded number of polls, until its
+predecessors have published their sums. The test hook fgc_debug_lookback
+shortens that bound and names a block that never publishes, so the waits of
+the blocks after it run out. The draw must then
 come back with FGC_ERR_DEVICE_LIMIT (not hang, not fault), leave the
 framebuffer untouched, keep its pending clears, and the same context must
 draw correctly once the hook is reset."""
@@ -28,8 +28,10 @@ def draw(lib, ctx, mh, st, sh):
 
 
 def test_lookback_wait_runs_out_and_context_stays_usable(gpu_lib):
-    w = h = 256
-    mesh = scenes.sphere_scene(4)  # 5,120 triangles: ten setup blocks of 512
+    # 81,920 triangles at 1920x1080: 540 bands x 20 binning blocks, a bin
+    # count matrix of six scan blocks
+    w, h = 1920, 1080
+    mesh = scenes.displaced_sphere(6)
     mh = _upload_mesh(mesh)
     sh = phong(scenes.camera_matrix(w, h), scenes.LIGHT, scenes.EYE, scenes.OBJECT_COLOR)
     st = state()
@@ -70,3 +72,6 @@ def test_default_lookback_limit_is_restored(gpu_lib):
     sh = phong(scenes.camera_matrix(640, 360), scenes.LIGHT, scenes.EYE, scenes.OBJECT_COLOR)
     rc, info = draw(gpu_lib, ctx, _upload_mesh(mesh), state(), sh)
     assert rc == _abi.FGC_OK and info[0] > 0
+    st = _abi.FgcStats()
+    _abi.check(gpu_lib.fgc_context_last_stats(ctx.handle, ctypes.byref(st)))
+    assert st.attempts == 1
