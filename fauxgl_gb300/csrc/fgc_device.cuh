@@ -154,10 +154,11 @@ __device__ __forceinline__ int64_t go_f2i(double f) {
     return INT64_MIN;
 }
 
-__device__ __forceinline__ bool dnan(double x) { return x != x; }
-__device__ __forceinline__ bool dinf(double x) { return fabs(x) == __longlong_as_double(0x7ff0000000000000LL); }
+// NaN, infinity and finiteness from the bits (fj_bits: integer pipe).
+__device__ __forceinline__ bool dnan(double x) { return (fj_bits(x) & 0x7fffffffffffffffull) > 0x7ff0000000000000ull; }
+__device__ __forceinline__ bool dinf(double x) { return (fj_bits(x) & 0x7fffffffffffffffull) == 0x7ff0000000000000ull; }
 __device__ __forceinline__ bool dfinite(double x) {
-    return ((unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull) < 0x7ff0000000000000ull;
+    return (fj_bits(x) & 0x7fffffffffffffffull) < 0x7ff0000000000000ull;
 }
 
 // math.Min / math.Max (explicit special cases: CUDA's fmin/fmax drop NaN).
@@ -189,7 +190,7 @@ __device__ __forceinline__ double go_clamp(double x, double lo, double hi) {
 constexpr unsigned long long kAbsMask = 0x7fffffffffffffffull;
 constexpr unsigned long long kInfBits = 0x7ff0000000000000ull;
 
-__device__ __forceinline__ unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
+__device__ __forceinline__ unsigned long long dbits(double x) { return (unsigned long long)fj_bits(x); }
 __device__ __forceinline__ bool bnan(unsigned long long b) { return (b & kAbsMask) > kInfBits; }
 // Total order on non-NaN doubles as unsigned keys (-0 sorts below +0).
 __device__ __forceinline__ unsigned long long okey(unsigned long long b) {
@@ -518,7 +519,7 @@ __device__ __forceinline__ double dot4(D4 a, D4 b) {
 // VectorW.Outside (vector.go:212-215): x < -w || x > w || ... with IEEE
 // comparisons (false for NaN, -0 == +0), evaluated on the integer pipe.
 __device__ __forceinline__ bool outside4(D4 a) {
-    const double nw = __longlong_as_double(__double_as_longlong(a.w) ^ (long long)0x8000000000000000ull);  // -w
+    const double nw = fj_double(dbits(a.w) ^ 0x8000000000000000ull);  // -w
     return dgt_i(nw, a.x) || dgt_i(a.x, a.w) || dgt_i(nw, a.y) || dgt_i(a.y, a.w) || dgt_i(nw, a.z) ||
            dgt_i(a.z, a.w);
 }

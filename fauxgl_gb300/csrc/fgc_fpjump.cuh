@@ -29,9 +29,15 @@
 
 namespace fgc {
 
+// The bit pattern of x. On the device it passes through an opaque move:
+// given a plain bit cast, the compiler turns masks, sign flips and compares of
+// the bits back into FP64 abs, negate and NaN tests (DADD / DSETP), which
+// issue on the FP64 pipe at the FP64 rate -- the pipe these helpers keep free.
 FGC_HD uint64_t fj_bits(double x) {
 #ifdef __CUDA_ARCH__
-    return (uint64_t)__double_as_longlong(x);
+    unsigned long long b;
+    asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+    return (uint64_t)b;
 #else
     uint64_t b;
     memcpy(&b, &x, 8);
@@ -41,7 +47,9 @@ FGC_HD uint64_t fj_bits(double x) {
 
 FGC_HD double fj_double(uint64_t b) {
 #ifdef __CUDA_ARCH__
-    return __longlong_as_double((long long)b);
+    double x;
+    asm("mov.b64 %0, %1;" : "=d"(x) : "l"((unsigned long long)b));
+    return x;
 #else
     double x;
     memcpy(&x, &b, 8);
