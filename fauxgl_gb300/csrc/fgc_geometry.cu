@@ -246,12 +246,16 @@ __device__ __forceinline__ bool clip_leaves_something(D4 a, D4 b, D4 c) {
 // 0 when culled.
 __device__ __forceinline__ int cull_decision(const StateView& st, double n0x, double n0y, double n1x, double n1y,
                                              double n2x, double n2y) {
-    double a = __dsub_rn(__dmul_rn(__dsub_rn(n1x, n0x), __dsub_rn(n2y, n0y)),
-                         __dmul_rn(__dsub_rn(n2x, n0x), __dsub_rn(n1y, n0y)));
-    int order = (a < 0) ? -1 : 1;
-    if (st.cull == FGC_CULL_FRONT) a = -a;
-    if (st.front_face == FGC_FACE_CW) a = -a;
-    if (st.cull != FGC_CULL_NONE && a <= 0) return 0;
+    const double a = __dsub_rn(__dmul_rn(__dsub_rn(n1x, n0x), __dsub_rn(n2y, n0y)),
+                               __dmul_rn(__dsub_rn(n2x, n0x), __dsub_rn(n1y, n0y)));
+    const int order = ic_lt0(a) ? -1 : 1;  // a < 0
+    // a = -a for a front-face cull and again for clockwise front faces (each
+    // flips the sign bit), then a <= 0: zero or negative, not NaN
+    const unsigned long long flip =
+        ((st.cull == FGC_CULL_FRONT) != (st.front_face == FGC_FACE_CW)) ? 0x8000000000000000ull : 0ull;
+    const unsigned long long b = dbits(a) ^ flip;
+    const bool le0 = !bnan(b) && ((b & kAbsMask) == 0 || (b >> 63) != 0);
+    if (st.cull != FGC_CULL_NONE && le0) return 0;
     return order;
 }
 
@@ -274,19 +278,12 @@ __device__ void emit_triangle(const GeomParams& P, const StateView& st, uint64_t
 // triangles, context.go:435-439), and the ordered allocation runs across all
 // of them, so every draw's primitives are one contiguous, ordered range.
 // Triangles take one slot (six in wireframe), or 7x that when they need
-// clipping; lines always take two slots (dead when clipped away). setup_kernel
-// decides culling and clipping and allocates; the surviving work items go to
-// a list that setup_emit_kernel turns into raster primitives, while the clip
-// kernels (on another stream) handle the clip entries.
+// clipping; lines always take two slots (dead when clipped away). The count
+// kernel decides culling and clipping (and lists the clipped triangles),
+// setup_kernel allocates; the surviving work items go to a list that
+// setup_emit_kernel turns into raster primitives, while the clip kernels (on
+// another stream) handle the clip entries.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void append_clip(const GeomParams& P, uint32_t item, uint64_t t, uint64_t slot) {
-    uint32_t idx = atomicAdd(P.clip_count, 1u);
-    if (idx < P.clip_cap) {
-        P.clip_list[idx] = ClipEntry{slot, (uint32_t)t, item};
-    } else {
-        atomicOr(P.status, ST_CLIP_OVERFLOW);
-    }
-}
 
 // One piece of a triangle that survived culling: the whole triangle, or in
 // wireframe its edge `piece` (two primitives at slot + 2*piece).
@@ -393,14 +390,22 @@ __global__ void __launch_bounds__(kSetupTile) setup_count_kernel(GeomParams P) {
     const SetupTileOf T = setup_tile_of(P, tile);
     const ItemView& I = P.items[T.item];
     const uint8_t* vout = P.vout + I.vbase;
-    uint16_t* meta = P.smeta + (uint64_t)tile * (kSetupTile * kSetupPer) + (uint64_t)kSetupPer * threadIdx.x;
+    const uint64_t e0 = (uint64_t)tile * (kSetupTile * kSetupPer) + (uint64_t)kSetupPer * threadIdx.x;
     uint32_t count = 0, work = 0;
 #pragma unroll
     for (int j = 0; j < kSetupPer; j++) {
         const SetupElem e = classify(P, I, T.tri, T.k0 + j, vout);
-        meta[j] = pack_meta(e);
+        P.smeta[e0 + j] = pack_meta(e);
         count += e.count;
         work += e.work;
+        if (T.tri && e.clip) {
+            // a clip entry now (its slot follows from the scan: the list
+            // writer fills it in), so that clipping starts before the scan
+            const uint32_t idx = atomicAdd(P.clip_count, 1u);
+            if (idx < P.clip_cap) P.clip_list[idx] = ClipEntry{~0ull, (uint32_t)(I.tri_first + T.k0 + j), T.item};
+            else atomicOr(P.status, ST_CLIP_OVERFLOW);
+            P.cidx[e0 + j] = idx;
+        }
     }
     uint64_t agg;
     block_exclusive_scan<kSetupTile>(((uint64_t)count << 31) | work, s_warp, &agg);
@@ -471,7 +476,8 @@ __global__ void __launch_bounds__(kSetupTile) setup_kernel(GeomParams P) {
         const uint64_t k = T.k0 + j;
         if (ecount != 0 && eclip) {
             if (tri) {
-                append_clip(P, T.item, I.tri_first + k, slot);
+                const uint32_t idx = P.cidx[(uint64_t)tile * (kSetupTile * kSetupPer) + (uint64_t)kSetupPer * threadIdx.x + j];
+                if (idx < P.clip_cap) P.clip_list[idx].slot = slot;  // the count kernel listed it
             } else {
                 uint32_t idx = atomicAdd(P.lclip_count, 1u);
                 P.lclip_list[idx] = ClipEntry{slot, (uint32_t)(I.line_first + k), T.item};  // holds every line of the pass
@@ -618,11 +624,16 @@ __device__ void interp_attrs(FullVertex& v, const FullVertex& a, const FullVerte
 }
 
 // FixNormals (triangle.go:46-58).
+// The face normal is formed only when a vertex normal is zero (== 0 as IEEE
+// compares, either sign): otherwise nothing reads it.
+__device__ __forceinline__ bool zero3(D3 v) { return dzero(v.x) && dzero(v.y) && dzero(v.z); }
 __device__ void fix_normals(FullVertex& a, FullVertex& b, FullVertex& c) {
-    D3 n = normalize3(cross3(sub3(b.pos, a.pos), sub3(c.pos, a.pos)));
-    if (a.nrm.x == 0 && a.nrm.y == 0 && a.nrm.z == 0) a.nrm = n;
-    if (b.nrm.x == 0 && b.nrm.y == 0 && b.nrm.z == 0) b.nrm = n;
-    if (c.nrm.x == 0 && c.nrm.y == 0 && c.nrm.z == 0) c.nrm = n;
+    const bool za = zero3(a.nrm), zb = zero3(b.nrm), zc = zero3(c.nrm);
+    if (!(za || zb || zc)) return;
+    const D3 n = normalize3(cross3(sub3(b.pos, a.pos), sub3(c.pos, a.pos)));
+    if (za) a.nrm = n;
+    if (zb) b.nrm = n;
+    if (zc) c.nrm = n;
 }
 
 __device__ FullVertex load_corner(const GeomParams& P, const ItemView& I, uint64_t corner) {
@@ -644,12 +655,23 @@ __device__ FullVertex load_corner(const GeomParams& P, const ItemView& I, uint64
     return v;
 }
 
-// ClipTriangle (clipping.go:54-74) + drawClippedTriangle for each piece.
-// Entry e owns primitive slots [base, base + 7*per) and pool vertices
-// [21e, 21e + 21).
-// One vertex of the clipped polygon as ClipTriangle builds it: barycentric
-// weights of its clip-space point w.r.t. the original triangle, then
-// InterpolateVertexes of Output and of the attributes the shader reads.
+// ClipTriangle (clipping.go:54-74) + drawClippedTriangle for each piece, in
+// three steps. Entry e owns primitive slots [base, base + 7*per) and pool
+// vertices [21e, 21e + 21).
+//   clip_poly_kernel    one thread per entry: sutherlandHodgman on the
+//                       corners' Output (clipping.go:28-52)
+//   clip_vert_kernel    one thread per polygon vertex: Barycentric weights of
+//                       its clip-space point w.r.t. the original triangle,
+//                       InterpolateVertexes of Output and of the attributes
+//                       the shader reads (clipping.go:61-65), its NDC position
+//   clip_piece_kernel   one thread per fan piece (0, i-1, i): the cull
+//                       decision, FixNormals of the piece's own copies and
+//                       the raster primitive (context.go:316-349)
+// The results are those of one thread doing all three in turn: each polygon
+// vertex is still built once and shared by the pieces that use it. The
+// kernels run on a side stream: the first two beside the scan and the list
+// writer, the third (it needs the slots the list writer assigns) beside the
+// emission.
 __device__ __forceinline__ FullVertex clip_vertex(const FullVertex* tv, D3 p1, D3 p2, D3 p3, D4 q, uint32_t mask) {
     const D4 bw = barycentric(p1, p2, p3, d3(q.x, q.y, q.z));
     FullVertex v;
@@ -658,20 +680,13 @@ __device__ __forceinline__ FullVertex clip_vertex(const FullVertex* tv, D3 p1, D
     return v;
 }
 
-__global__ void __launch_bounds__(128) clip_triangles_kernel(GeomParams P) {
-    uint32_t n = min(*P.clip_count, P.clip_cap);
+__global__ void __launch_bounds__(32) clip_poly_kernel(GeomParams P) {
+    const uint32_t n = min(*P.clip_count, P.clip_cap);
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
         const ClipEntry ent = P.clip_list[e];
         const ItemView& I = P.items[ent.item];
-        const uint64_t t = ent.elem, base = ent.slot;
-        const int per = I.st.wireframe ? 6 : 1;
-        const uint32_t mask = I.attr_mask;
-        FullVertex tv[3];
-        for (int c = 0; c < 3; c++) tv[c] = load_corner(P, I, 3 * t + c);
-        if (mask & kAttrNrm) fix_normals(tv[0], tv[1], tv[2]);  // NewTriangle(v1, v2, v3)
-        D3 p1 = d3(tv[0].out.x, tv[0].out.y, tv[0].out.z);
-        D3 p2 = d3(tv[1].out.x, tv[1].out.y, tv[1].out.z);
-        D3 p3 = d3(tv[2].out.x, tv[2].out.y, tv[2].out.z);
+        const uint64_t t = ent.elem;
+        const VClip* vc = P.vclip + I.vbase;
         // sutherlandHodgman (clipping.go:28-52). Each plane adds at most one
         // vertex to a convex polygon (9 after six planes); the buffers hold 16
         // and drop vertices beyond that, which only a polygon made non-convex
@@ -679,7 +694,10 @@ __global__ void __launch_bounds__(128) clip_triangles_kernel(GeomParams P) {
         // plane is computed once and reused as the next edge's start.
         constexpr int kPolyMax = 16;
         D4 bufa[kPolyMax], bufb[kPolyMax];
-        bufa[0] = tv[0].out; bufa[1] = tv[1].out; bufa[2] = tv[2].out;
+        for (int c = 0; c < 3; c++) {
+            const VClip o = vc[I.mesh.corner_uniq[3 * t + c]];
+            bufa[c] = d4(o.x, o.y, o.z, o.w);
+        }
         int nin = 3;
         D4* in = bufa;
         D4* out = bufb;
@@ -700,56 +718,95 @@ __global__ void __launch_bounds__(128) clip_triangles_kernel(GeomParams P) {
             D4* tmp = in; in = out; out = tmp;
             nin = no;
         }
-        // the fan (0, i-1, i): each polygon vertex is built once and shared by
-        // the pieces that use it; FixNormals acts on each piece's own copies
-        // (NewTriangle of fresh vertices, clipping.go:66-72)
-        int sub = 0;
-        if (nin >= 3) {
-            const FullVertex va = clip_vertex(tv, p1, p2, p3, in[0], mask);
-            const D3 na = ndc_of(va.out);
-            FullVertex vb = clip_vertex(tv, p1, p2, p3, in[1], mask);
-            D3 nb = ndc_of(vb.out);
-            for (int i = 2; i < nin && sub < 7; i++, sub++) {
-                const FullVertex vc = clip_vertex(tv, p1, p2, p3, in[i], mask);
-                const D3 nc = ndc_of(vc.out);
-                // drawClippedTriangle (context.go:316-349)
-                const int order = cull_decision(I.st, na.x, na.y, nb.x, nb.y, nc.x, nc.y);
-                const uint64_t slot = base + (uint64_t)sub * per;
-                if (order == 0) {
-                    for (int q = 0; q < per; q++) write_dead(P, slot + q);
-                } else {
-                    FullVertex v[3] = {va, vb, vc};
-                    if (mask & kAttrNrm) fix_normals(v[0], v[1], v[2]);  // NewTriangle
-                    uint32_t pref[3];
-                    for (int c = 0; c < 3; c++) {
-                        uint32_t pi = e * 21 + sub * 3 + c;
-                        if (mask) {
-                            P.pool[pi] = PoolVertex{v[c].pos.x, v[c].pos.y, v[c].pos.z, v[c].nrm.x, v[c].nrm.y,
-                                                    v[c].nrm.z, v[c].tu, v[c].tv, v[c].col.x, v[c].col.y,
-                                                    v[c].col.z, v[c].col.w};
-                            if (I.st.precision == FGC_PRECISION_MIXED)
-                                P.pool32[pi] = PoolVertex32{(float)v[c].pos.x, (float)v[c].pos.y, (float)v[c].pos.z,
-                                                            (float)v[c].nrm.x, (float)v[c].nrm.y, (float)v[c].nrm.z,
-                                                            (float)v[c].tu, (float)v[c].tv, (float)v[c].col.x,
-                                                            (float)v[c].col.y, (float)v[c].col.z, (float)v[c].col.w};
-                        }
-                        pref[c] = kPoolFlag | pi;
-                    }
-                    int i0 = 0, i2 = 2;
-                    if (order < 0) { i0 = 2; i2 = 0; }
-                    D3 nn[3] = {na, nb, nc};
-                    D3 s0 = screen_of_ndc(nn[i0], I.w2, I.h2);
-                    D3 s1 = screen_of_ndc(nn[1], I.w2, I.h2);
-                    D3 s2 = screen_of_ndc(nn[i2], I.w2, I.h2);
-                    emit_triangle(P, I.st, slot, s0, s1, s2, __drcp_rn(v[i0].out.w), __drcp_rn(v[1].out.w),
-                                  __drcp_rn(v[i2].out.w), pref[i0], pref[1], pref[i2], (uint32_t)t);
-                }
-                vb = vc;
-                nb = nc;
-            }
+        ClipPoly& cp = P.cpoly[e];
+        cp.n = (uint32_t)nin;
+        for (int j = 0; j < nin && j < kClipPoly; j++) cp.v[j] = make_double4(in[j].x, in[j].y, in[j].z, in[j].w);
+    }
+}
+
+__global__ void __launch_bounds__(64) clip_vert_kernel(GeomParams P) {
+    const uint64_t n = (uint64_t)min(*P.clip_count, P.clip_cap) * kClipPoly;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t e = (uint32_t)(i / kClipPoly), j = (uint32_t)(i % kClipPoly);
+        const uint32_t np = P.cpoly[e].n;
+        if (np < 3 || j >= np) continue;  // no fan, or a vertex the fan does not read
+        const ClipEntry ent = P.clip_list[e];
+        const ItemView& I = P.items[ent.item];
+        const uint32_t mask = I.attr_mask;
+        FullVertex tv[3];
+        for (int c = 0; c < 3; c++) tv[c] = load_corner(P, I, 3 * (uint64_t)ent.elem + c);
+        if (mask & kAttrNrm) fix_normals(tv[0], tv[1], tv[2]);  // NewTriangle(v1, v2, v3)
+        const D3 p1 = d3(tv[0].out.x, tv[0].out.y, tv[0].out.z);
+        const D3 p2 = d3(tv[1].out.x, tv[1].out.y, tv[1].out.z);
+        const D3 p3 = d3(tv[2].out.x, tv[2].out.y, tv[2].out.z);
+        const double4 q = P.cpoly[e].v[j];
+        const FullVertex v = clip_vertex(tv, p1, p2, p3, d4(q.x, q.y, q.z, q.w), mask);
+        const D3 nd = ndc_of(v.out);
+        P.cvert[i] = ClipVert{v.pos.x, v.pos.y, v.pos.z, v.nrm.x, v.nrm.y, v.nrm.z, v.tu, v.tv,
+                              v.col.x, v.col.y, v.col.z, v.col.w, v.out.x, v.out.y, v.out.z, v.out.w,
+                              nd.x, nd.y, nd.z};
+    }
+}
+
+__device__ __forceinline__ FullVertex clip_vert_load(const ClipVert& c, D3& nd) {
+    FullVertex v;
+    v.pos = d3(c.px, c.py, c.pz);
+    v.nrm = d3(c.nx, c.ny, c.nz);
+    v.tu = c.tu;
+    v.tv = c.tv;
+    v.tz = 0.0;
+    v.col = d4(c.cr, c.cg, c.cb, c.ca);
+    v.out = d4(c.ox, c.oy, c.oz, c.ow);
+    nd = d3(c.sx, c.sy, c.sz);
+    return v;
+}
+
+__global__ void __launch_bounds__(64) clip_piece_kernel(GeomParams P) {
+    const uint64_t n = (uint64_t)min(*P.clip_count, P.clip_cap) * 7;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t e = (uint32_t)(i / 7), sub = (uint32_t)(i % 7);
+        const ClipEntry ent = P.clip_list[e];
+        const ItemView& I = P.items[ent.item];
+        const int per = I.st.wireframe ? 6 : 1;
+        const uint64_t slot = ent.slot + (uint64_t)sub * per;
+        const uint32_t np = P.cpoly[e].n;
+        if (np < 3 || sub + 2 >= np) {  // the fan (0, i-1, i), i = 2 .. np-1, has no piece here
+            for (int q = 0; q < per; q++) write_dead(P, slot + q);
+            continue;
         }
-        for (; sub < 7; sub++)
-            for (int q = 0; q < per; q++) write_dead(P, base + (uint64_t)sub * per + q);
+        const uint32_t mask = I.attr_mask;
+        const ClipVert* cv = P.cvert + (uint64_t)e * kClipPoly;
+        D3 nn[3];
+        FullVertex v[3] = {clip_vert_load(cv[0], nn[0]), clip_vert_load(cv[sub + 1], nn[1]),
+                           clip_vert_load(cv[sub + 2], nn[2])};
+        // drawClippedTriangle (context.go:316-349)
+        const int order = cull_decision(I.st, nn[0].x, nn[0].y, nn[1].x, nn[1].y, nn[2].x, nn[2].y);
+        if (order == 0) {
+            for (int q = 0; q < per; q++) write_dead(P, slot + q);
+            continue;
+        }
+        if (mask & kAttrNrm) fix_normals(v[0], v[1], v[2]);  // NewTriangle
+        uint32_t pref[3];
+        for (int c = 0; c < 3; c++) {
+            const uint32_t pi = e * 21 + sub * 3 + c;
+            if (mask) {
+                P.pool[pi] = PoolVertex{v[c].pos.x, v[c].pos.y, v[c].pos.z, v[c].nrm.x, v[c].nrm.y, v[c].nrm.z,
+                                        v[c].tu, v[c].tv, v[c].col.x, v[c].col.y, v[c].col.z, v[c].col.w};
+                if (I.st.precision == FGC_PRECISION_MIXED)
+                    P.pool32[pi] = PoolVertex32{(float)v[c].pos.x, (float)v[c].pos.y, (float)v[c].pos.z,
+                                                (float)v[c].nrm.x, (float)v[c].nrm.y, (float)v[c].nrm.z,
+                                                (float)v[c].tu, (float)v[c].tv, (float)v[c].col.x,
+                                                (float)v[c].col.y, (float)v[c].col.z, (float)v[c].col.w};
+            }
+            pref[c] = kPoolFlag | pi;
+        }
+        int i0 = 0, i2 = 2;
+        if (order < 0) { i0 = 2; i2 = 0; }
+        const D3 s0 = screen_of_ndc(nn[i0], I.w2, I.h2);
+        const D3 s1 = screen_of_ndc(nn[1], I.w2, I.h2);
+        const D3 s2 = screen_of_ndc(nn[i2], I.w2, I.h2);
+        emit_triangle(P, I.st, slot, s0, s1, s2, __drcp_rn(v[i0].out.w), __drcp_rn(v[1].out.w),
+                      __drcp_rn(v[i2].out.w), pref[i0], pref[1], pref[i2], (uint32_t)ent.elem);
     }
 }
 

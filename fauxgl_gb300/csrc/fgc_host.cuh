@@ -215,6 +215,8 @@ struct PassScratch {
     DevBuf<ClipEntry> clip_list, lclip_list;
     DevBuf<PoolVertex> pool;
     DevBuf<PoolVertex32> pool32;
+    DevBuf<ClipPoly> cpoly;        // per clip_list entry: its clipped polygon
+    DevBuf<ClipVert> cvert;        // per clip_list entry: the polygon's vertices
     DevBuf<uint32_t> mat, off, bins;
     DevBuf<uint32_t> pnb, prs;     // per primitive: bands it is binned to, first row-start slot
     DevBuf<double> rstart;         // per (primitive, band): edge values at its first row in the band
@@ -223,6 +225,7 @@ struct PassScratch {
     DevBuf<double> dbg;
     DevBuf<SetupWork> work;        // setup work items (triangles, wireframe edges, lines)
     DevBuf<uint16_t> smeta;        // per element of a setup tile: its setup decision
+    DevBuf<uint32_t> cidx;         // per element of a setup tile: its clip_list entry (clipped triangles)
     DevBuf<unsigned long long> tsum;  // per setup tile: its sums, then their exclusive prefix
     PinnedBuf host_in, host_out;
     uint32_t clip_cap = 1024;
@@ -230,7 +233,7 @@ struct PassScratch {
     // the clip kernels run on a second stream beside the setup emission
     int side_device = -1;
     cudaStream_t side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_clip = nullptr, ev_join = nullptr;
     PassScratch() = default;
     PassScratch(const PassScratch&) = delete;
     PassScratch& operator=(const PassScratch&) = delete;

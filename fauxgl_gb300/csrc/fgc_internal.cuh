@@ -96,6 +96,20 @@ struct __align__(16) ClipEntry {
     uint32_t item;
 };
 
+// Clipped triangles pass through three kernels: the polygon of each after
+// the six planes (clip space), then each polygon vertex with its
+// interpolated attributes and NDC position.
+constexpr int kClipPoly = 9;  // polygon vertices the fan reads (7 pieces)
+struct __align__(16) ClipPoly {
+    double4 v[kClipPoly];
+    uint32_t n;                 // vertices of the clipped polygon (the fan reads the first kClipPoly)
+};
+struct __align__(16) ClipVert {
+    double px, py, pz, nx, ny, nz, tu, tv, cr, cg, cb, ca;  // attributes, as a clip pool vertex
+    double ox, oy, oz, ow;      // Output (clip space)
+    double sx, sy, sz;          // NDC
+};
+
 struct VertexParams {
     const ItemView* items;
     ItemStarts starts;
@@ -130,6 +144,8 @@ struct GeomParams {
     uint32_t* lclip_count;
     PoolVertex* pool;           // 21 per clip_list entry
     PoolVertex32* pool32;       // FP32 copies (draws in the mixed form)
+    ClipPoly* cpoly;            // per clip_list entry
+    ClipVert* cvert;            // kClipPoly per clip_list entry
     unsigned long long* prim_total;
     Lookback lb;
     unsigned int* status;
@@ -137,6 +153,7 @@ struct GeomParams {
     uint64_t work_cap;
     unsigned long long* work_total;
     uint16_t* smeta;            // per element of a setup tile: its setup decision (setup_count -> setup_kernel)
+    uint32_t* cidx;             // per element of a setup tile: its clip_list entry, for a clipped triangle
     unsigned long long* tsum;   // per setup tile: slots << 31 | work items, then their exclusive prefix
 };
 constexpr int kSetupTile = 256;  // threads of a setup tile
@@ -243,7 +260,9 @@ __global__ void setup_count_kernel(GeomParams P);
 __global__ void setup_scan_kernel(GeomParams P);
 __global__ void setup_kernel(GeomParams P);
 __global__ void setup_emit_kernel(GeomParams P);
-__global__ void clip_triangles_kernel(GeomParams P);
+__global__ void clip_poly_kernel(GeomParams P);
+__global__ void clip_vert_kernel(GeomParams P);
+__global__ void clip_piece_kernel(GeomParams P);
 __global__ void clip_lines_kernel(GeomParams P);
 
 __global__ void bin_count_kernel(BinParams P);

@@ -316,6 +316,8 @@ int plan_submission(PassScratch& S, const DevLimits& D, const PassTuning& T, con
     FGC_CUDA(S.clip_list.ensure(S.clip_cap));
     FGC_CUDA(S.pool.ensure((size_t)S.clip_cap * 21));
     FGC_CUDA(S.pool32.ensure((size_t)S.clip_cap * 21));
+    FGC_CUDA(S.cpoly.ensure(S.clip_cap));
+    FGC_CUDA(S.cvert.ensure((size_t)S.clip_cap * kClipPoly));
     FGC_CUDA(S.lclip_list.ensure(need_lines));
     FGC_CUDA(S.mat.ensure(need_mat));
     FGC_CUDA(S.off.ensure(need_mat));
@@ -328,22 +330,25 @@ int plan_submission(PassScratch& S, const DevLimits& D, const PassTuning& T, con
     uint64_t need_stiles = 1;
     for (const PassPlan& P : plans) need_stiles = std::max<uint64_t>(need_stiles, P.stiles);
     FGC_CUDA(S.smeta.ensure(need_stiles * kSetupTile * kSetupPer));
+    FGC_CUDA(S.cidx.ensure(need_stiles * kSetupTile * kSetupPer));
     FGC_CUDA(S.tsum.ensure(need_stiles));
     FGC_CUDA(S.table.ensure(TL.total));
     int dev = 0;
     FGC_CUDA(cudaGetDevice(&dev));
     if (!S.side || S.side_device != dev) {
         if (S.ev_fork) cudaEventDestroy(S.ev_fork);
+        if (S.ev_clip) cudaEventDestroy(S.ev_clip);
         if (S.ev_join) cudaEventDestroy(S.ev_join);
         if (S.side) cudaStreamDestroy(S.side);
         S.side = nullptr;
-        S.ev_fork = S.ev_join = nullptr;
-        // the highest priority: the clip kernel's few blocks are placed before
-        // the emission's fill the SMs
+        S.ev_fork = S.ev_clip = S.ev_join = nullptr;
+        // the highest priority: the clip kernels' few blocks are placed
+        // before the main stream's fill the SMs
         int least = 0, greatest = 0;
         FGC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
         FGC_CUDA(cudaStreamCreateWithPriority(&S.side, cudaStreamNonBlocking, greatest));
         FGC_CUDA(cudaEventCreateWithFlags(&S.ev_fork, cudaEventDisableTiming));
+        FGC_CUDA(cudaEventCreateWithFlags(&S.ev_clip, cudaEventDisableTiming));
         FGC_CUDA(cudaEventCreateWithFlags(&S.ev_join, cudaEventDisableTiming));
         S.side_device = dev;
     }
@@ -468,6 +473,8 @@ int issue_submission(PassScratch& S, cudaStream_t stream, const DevLimits& D, co
         gp.lclip_count = &dc->lclip_count;
         gp.pool = S.pool.p;
         gp.pool32 = S.pool32.p;
+        gp.cpoly = S.cpoly.p;
+        gp.cvert = S.cvert.p;
         gp.prim_total = &dc->prim_total;
         gp.lb = draw_lookback(t_setup, &dc->tick_setup, status, nullptr);  // setup_kernel writes the totals
         gp.status = status;
@@ -475,30 +482,42 @@ int issue_submission(PassScratch& S, cudaStream_t stream, const DevLimits& D, co
         gp.work_cap = S.work.cap;
         gp.work_total = &dc->work_total;
         gp.smeta = S.smeta.p;
+        gp.cidx = S.cidx.p;
         gp.tsum = S.tsum.p;
+        // Clipped triangles: the count kernel lists them, and on the side
+        // stream one kernel builds their polygons and one the polygons'
+        // vertices while the scan and the list writer run; a third makes the
+        // fan pieces beside the emission (they need the slots the list writer
+        // assigns). Clipped lines are listed by the list writer and clipped
+        // beside the emission as well.
+        const bool clips = P.any_tri || P.any_line;
         setup_count_kernel<<<P.stiles, kSetupTile, 0, stream>>>(gp);
+        if (P.any_tri) {
+            FGC_CUDA(cudaEventRecord(S.ev_fork, stream));
+            FGC_CUDA(cudaStreamWaitEvent(S.side, S.ev_fork, 0));
+            // one warp per block: a few thousand clip entries still spread
+            // over every SM's FP64 pipes
+            clip_poly_kernel<<<grid_for(S.clip_cap, 32, D.sms * 8), 32, 0, S.side>>>(gp);
+            clip_vert_kernel<<<grid_for((uint64_t)S.clip_cap * kClipPoly, 64, D.sms * 8), 64, 0, S.side>>>(gp);
+            FGC_CUDA(cudaGetLastError());
+            rec.launches += 2;
+        }
         setup_scan_kernel<<<1, 1024, 0, stream>>>(gp);
         setup_kernel<<<P.stiles, kSetupTile, 0, stream>>>(gp);
         FGC_CUDA(cudaGetLastError());
         rec.launches += 3;
-        // the clip kernels (latency-bound: one long FP64 chain per entry) run
-        // on the side stream while the emission fills every SM's FP64 pipe
-        const bool clips = P.any_tri || P.any_line;
         if (clips) {
-            FGC_CUDA(cudaEventRecord(S.ev_fork, stream));
-            FGC_CUDA(cudaStreamWaitEvent(S.side, S.ev_fork, 0));
+            FGC_CUDA(cudaEventRecord(S.ev_clip, stream));
+            FGC_CUDA(cudaStreamWaitEvent(S.side, S.ev_clip, 0));
             if (P.any_tri) {
-                // one warp per block: a few thousand clip entries still spread
-                // over every SM's FP64 pipes
-                clip_triangles_kernel<<<grid_for(S.clip_cap, 32, D.sms * 8), 32, 0, S.side>>>(gp);
-                FGC_CUDA(cudaGetLastError());
+                clip_piece_kernel<<<grid_for((uint64_t)S.clip_cap * 7, 64, D.sms * 8), 64, 0, S.side>>>(gp);
                 rec.launches++;
             }
             if (P.any_line) {
                 clip_lines_kernel<<<grid_for(P.nlines, 128, D.sms * 4), 128, 0, S.side>>>(gp);
-                FGC_CUDA(cudaGetLastError());
                 rec.launches++;
             }
+            FGC_CUDA(cudaGetLastError());
             FGC_CUDA(cudaEventRecord(S.ev_join, S.side));
         }
         setup_emit_kernel<<<grid_for(P.work_items, 256, D.sms * 16), 256, 0, stream>>>(gp);
