@@ -1044,8 +1044,11 @@ def main():
                          "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
                                             "profiles/raster_kernel_dense1080p.json (%s)" % prof.get("version", "?"))
                          if prof else None,
-                         "peak_source": "FP64 add rate measured in this run by the library's own probe "
-                                        "(fgc_measure_fp64_rate; the pool's MEASURED_PEAKS.json has no FP64 figure)",
+                         "peak_source": "FP64 add (DADD) rate measured in this run by the library's own probe "
+                                        "(fgc_measure_fp64_rate): the issue rate of the adds and multiplies the "
+                                        "reference's arithmetic consists of, 84 % of ncu's FP64 pipe peak (which only "
+                                        "DFMAs of general operands reach); the pool's MEASURED_PEAKS.json has no FP64 "
+                                        "figure",
                          "flops_per_launch": int(flops),
                          "hbm": {"bound_of": "whole frame", "algorithmic_bytes": int(frame_bytes),
                                  "achieved": round(frame_bytes / (ms * 1e-3) / 1e9, 1),
