@@ -285,8 +285,9 @@ int fgc_context_set_stream(fgc_context* ctx, void* cuda_stream);
 int fgc_debug_lookback(uint32_t spin_limit, uint32_t withhold_block);
 /* FP64 pipe throughput of the current device, measured: independent FP64
  * adds issued on every SM, in G instructions per second. It is the roofline
- * denominator of the FP64-bound stages (one add, multiply or compare is one
- * instruction). */
+ * denominator of the FP64-bound stages, whose arithmetic is adds and
+ * multiplies (both issue at this rate; a fused multiply-add of general
+ * operands issues about 1.19x faster). */
 int fgc_measure_fp64_rate(double* gops_per_s);
 
 /* ---- batches (no reference counterpart) --------------------------------- */
