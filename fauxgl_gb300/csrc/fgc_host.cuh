@@ -230,7 +230,8 @@ struct PassScratch {
     PinnedBuf host_in, host_out;
     uint32_t clip_cap = 1024;
     uint64_t bin_cap = 0;
-    // the clip kernels run on a second stream beside the setup emission
+    // the clip kernels run on a second stream beside the setup scan, list
+    // writer and emission
     int side_device = -1;
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_clip = nullptr, ev_join = nullptr;

@@ -5,12 +5,19 @@
 // A pass, no host wait inside:
 //   table upload              item views + lookup starts (pinned -> device)
 //   vertex_kernel             per draw, per unique position
-//   setup_kernel              draw by draw, triangles then lines, one ordered
-//                             allocation across the pass (slots and work items)
+//   setup_count_kernel        draw by draw, triangles then lines: culling and
+//                             clipping decisions, per-tile sums; lists the
+//                             clipped triangles
+//   setup_scan_kernel         one block: the tile prefix, the pass totals
+//   setup_kernel              the ordered allocation across the pass (slots
+//                             and work items), clipped lines listed
 //   setup_emit_kernel         the work items' raster primitives and each draw's
-//                             primitive range; beside it, on a second stream,
-//   clip_triangles / clip_lines_kernel
+//                             primitive range
+//   on a second stream: clip_poly / clip_vert_kernel (from the count kernel
+//   on), clip_piece / clip_lines_kernel (from the list writer on), joined
+//   before binning
 //   bin_count / scan_u32 / bin_scatter   per-draw band bins, one scan
+//   scan_u32 / row_starts_kernel         (draws with tall primitives)
 //   raster_kernel             persistent CTAs over the pass's (draw, band)
 //                             queue
 //   result copy               status, counters, per-draw RasterizeInfo
