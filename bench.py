@@ -211,6 +211,7 @@ class Frame:
         self.pass_work = [None, None]
         self.bg = (ctypes.c_double * 4)(*scenes.BACKGROUND)
         self.info = _abi.FgcRasterizeInfo()
+        self.launches = 0
         self.ds = None
         if scale > 1:
             import numpy as np
@@ -229,37 +230,47 @@ class Frame:
         _abi.check(self.lib.fgc_context_last_stats(self.ctx, ctypes.byref(s)))
         return s
 
-    def run(self):
+    def run(self, record=True):
+        """One frame: clears, the draw(s), the downsample. With record, also the
+        draws' statistics (stage times, work, kernel launches); without, only
+        the library calls (the timed frames), and the launches of the last
+        recorded frame are returned."""
         from fauxgl_gb300 import _abi
         lib = self.lib
         _abi.check(lib.fgc_clear_color(self.ctx, self.bg))
         _abi.check(lib.fgc_clear_depth(self.ctx, 1.7976931348623157e308))
         _abi.check(lib.fgc_draw_mesh(self.ctx, self.mesh_h, ctypes.byref(self.st), ctypes.byref(self.sh),
                                      ctypes.byref(self.info)))
-        s = self.stats()
-        launches = s.kernel_launches
-        self.pass_ms[0] = [a + b for a, b in zip(self.pass_ms[0], s.stage_ms)]
-        self.pass_work[0] = work_dict(s)
+        if record:
+            s = self.stats()
+            launches = s.kernel_launches
+            self.pass_ms[0] = [a + b for a, b in zip(self.pass_ms[0], s.stage_ms)]
+            self.pass_work[0] = work_dict(s)
         if self.overlay:
             _abi.check(lib.fgc_draw_mesh(self.ctx, self.mesh_h, ctypes.byref(self.st2), ctypes.byref(self.sh2),
                                          ctypes.byref(self.info)))
-            s = self.stats()
-            launches += s.kernel_launches
-            self.pass_ms[1] = [a + b for a, b in zip(self.pass_ms[1], s.stage_ms)]
-            self.pass_work[1] = work_dict(s)
+            if record:
+                s = self.stats()
+                launches += s.kernel_launches
+                self.pass_ms[1] = [a + b for a, b in zip(self.pass_ms[1], s.stage_ms)]
+                self.pass_work[1] = work_dict(s)
         if self.ds is not None:
             _abi.check(lib.fgc_downsample(self.ctx, self.scale,
                                           self.ds.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))))
-            launches += 1
-        return launches
+            if record:
+                launches += 1
+        if record:
+            self.launches = launches
+        return self.launches
 
     def close(self):
         self.lib.fgc_context_destroy(self.ctx)
 
 
-def time_frames(frame, steps, warmup, torch, dist_barrier, stage_acc=None):
+def time_frames(frame, steps, warmup, torch, dist_barrier, stage_acc=None, record=False):
     """Device-timed frames on torch's current stream (the library launches on
-    it). Returns (ms per frame, launches per frame)."""
+    it). Returns (ms per frame, launches per frame). The timed frames read the
+    draws' statistics only with stage_acc or record."""
     stream = torch.cuda.current_stream()
     frame.set_stream(stream.cuda_stream)
     for _ in range(warmup):
@@ -271,7 +282,7 @@ def time_frames(frame, steps, warmup, torch, dist_barrier, stage_acc=None):
     launches = 0
     e0.record(stream)
     for _ in range(steps):
-        launches += frame.run()
+        launches += frame.run(record=record or stage_acc is not None)
         if stage_acc is not None:
             s = frame.stats()
             for i in range(5):
@@ -971,7 +982,7 @@ def main():
         for name, prec in (("plain", _abi.FGC_PRECISION_PLAIN), ("mixed", _abi.FGC_PRECISION_MIXED)):
             f = Frame(lib, mesh_h, W * SS, H * SS, prec, overlay=True, scale=SS)
             f.set_timing(True)
-            ss_ms, ss_launch = time_frames(f, args.ss_steps, 1, torch, barrier)
+            ss_ms, ss_launch = time_frames(f, args.ss_steps, 1, torch, barrier, record=True)
             n = args.ss_steps + 1
             ss[name] = {"value": round(1e3 / ss_ms, 3), "unit": "frames/s", "ms_per_frame": round(ss_ms, 3),
                         "stages_ms": {"surface": {k: round(v / n, 3) for k, v in zip(_abi.STAGE_NAMES, f.pass_ms[0])},
