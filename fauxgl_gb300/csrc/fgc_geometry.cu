@@ -720,7 +720,7 @@ __global__ void __launch_bounds__(32) clip_poly_kernel(GeomParams P) {
         }
         ClipPoly& cp = P.cpoly[e];
         cp.n = (uint32_t)nin;
-        for (int j = 0; j < nin && j < kClipPoly; j++) cp.v[j] = make_double4(in[j].x, in[j].y, in[j].z, in[j].w);
+        for (int j = 0; j < nin && j < kClipPoly; j++) cp.v[j] = in[j];
     }
 }
 
@@ -739,8 +739,7 @@ __global__ void __launch_bounds__(64) clip_vert_kernel(GeomParams P) {
         const D3 p1 = d3(tv[0].out.x, tv[0].out.y, tv[0].out.z);
         const D3 p2 = d3(tv[1].out.x, tv[1].out.y, tv[1].out.z);
         const D3 p3 = d3(tv[2].out.x, tv[2].out.y, tv[2].out.z);
-        const double4 q = P.cpoly[e].v[j];
-        const FullVertex v = clip_vertex(tv, p1, p2, p3, d4(q.x, q.y, q.z, q.w), mask);
+        const FullVertex v = clip_vertex(tv, p1, p2, p3, P.cpoly[e].v[j], mask);
         const D3 nd = ndc_of(v.out);
         P.cvert[i] = ClipVert{v.pos.x, v.pos.y, v.pos.z, v.nrm.x, v.nrm.y, v.nrm.z, v.tu, v.tv,
                               v.col.x, v.col.y, v.col.z, v.col.w, v.out.x, v.out.y, v.out.z, v.out.w,

@@ -101,7 +101,7 @@ struct __align__(16) ClipEntry {
 // interpolated attributes and NDC position.
 constexpr int kClipPoly = 9;  // polygon vertices the fan reads (7 pieces)
 struct __align__(16) ClipPoly {
-    double4 v[kClipPoly];
+    D4 v[kClipPoly];
     uint32_t n;                 // vertices of the clipped polygon (the fan reads the first kClipPoly)
 };
 struct __align__(16) ClipVert {
