@@ -1330,16 +1330,22 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
             const uint64_t ucap = direct ? (uint64_t)min(F, kRT) : (uint64_t)P.su;
             const int jmax = split ? (threadIdx.x == 0 ? 1 : 0) : kChunkPer;
             if (split && threadIdx.x == 0) ce[0].nrows = (int32_t)split;
+            // the fragment estimates and the units in one scan (estimates in
+            // the high half, units in the low half). An entry whose estimate
+            // is above F, or whose rows are more than the chunk's units, ends
+            // the chunk wherever it stands, so each value is capped at one
+            // above its limit: every comparison below is unchanged, and both
+            // sums stay far below 2^32 (256 entries per chunk)
             uint64_t tkey = 0, tun = 0;
 #pragma unroll
             for (int j = 0; j < kChunkPer; j++) {
                 if (j >= jmax) break;
-                tkey += chunk_key(ce[j], direct, ratio, F);
-                tun += (uint64_t)ce[j].nrows;
+                tkey += min(chunk_key(ce[j], direct, ratio, F), (uint64_t)F + 1);
+                tun += min((uint64_t)ce[j].nrows, ucap + 1);
             }
-            uint64_t kagg, uagg;
-            uint64_t kr = block_exclusive_scan<kRT>(tkey, s_warp, &kagg);
-            uint64_t ur = block_exclusive_scan<kRT>(tun, s_warp, &uagg);
+            uint64_t pagg;
+            const uint64_t pr = block_exclusive_scan<kRT>((tkey << 32) | tun, s_warp, &pagg);
+            uint64_t kr = pr >> 32, ur = pr & 0xffffffffull;
             // the entries inside the prefix (never empty: the first entry's
             // rows fit, and a direct chunk's first estimate is at most its
             // bound <= F)
@@ -1349,7 +1355,7 @@ __global__ void __launch_bounds__(kRT, 2) raster_kernel(RasterParams P) {
 #pragma unroll
                 for (int j = 0; j < kChunkPer; j++) {
                     if (j >= jmax) break;
-                    const uint64_t key = chunk_key(ce[j], direct, ratio, F);
+                    const uint64_t key = min(chunk_key(ce[j], direct, ratio, F), (uint64_t)F + 1);
                     if (e0 + j >= bcount || ur + (uint64_t)ce[j].nrows > ucap || kr + key > (uint64_t)F) break;
                     const uint32_t slot = threadIdx.x * kChunkPer + j;
                     S.cprim[slot] = ce[j].p;
