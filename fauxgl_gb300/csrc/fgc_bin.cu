@@ -71,57 +71,89 @@ __global__ void __launch_bounds__(256) bin_count_kernel(BinParams P) {
     for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) P.mat[B.mat0 + (uint64_t)i * B.nblk + B.lblk] = hist[i];
 }
 
-// Row starts of every (primitive, band) pair: one thread per primitive walks
-// its rows downward, adding b12 per row as rasterize does (context.go:275-277),
-// and records the edge values at its first row in each of its bands (the
-// first row of the box whose index range meets the band, as the raster stage
-// counts them). Gaps above 64 rows are crossed with exact jumps.
+// Row starts of every (primitive, band) pair: the edge values at its first
+// row in each of its bands (the first row of the box whose index range meets
+// the band, as the raster stage counts them), by the reference's per-row
+// adds b12 from the primitive's top row (context.go:275-277). A block takes
+// 256 primitives and splits each one's bands into segments of kRowSeg; one
+// thread per segment jumps from the top row to the segment's first row (the
+// exact serial sum, fgc_fpjump.cuh) and adds row by row from there, so a
+// tall primitive no longer holds its warp while the others' lanes idle.
+// Gaps above 64 rows between bands are crossed with exact jumps as well.
+constexpr uint32_t kRowSeg = 8;
+
+__device__ __forceinline__ double row_advance(double w, double b, int64_t gap) {
+    if (gap > 64) return repeat_add(w, b, (uint64_t)gap);
+    for (int64_t j = 0; j < gap; j++) w = __dadd_rn(w, b);
+    return w;
+}
+
 __global__ void __launch_bounds__(256) row_starts_kernel(RowStartParams P) {
-    if (*P.status & (kRetryBits | ST_BIN_OVERFLOW)) return;
+    __shared__ uint32_t s_seg[256];     // per primitive of the tile: its first segment
+    __shared__ uint64_t s_warp[256 / 32 + 1];
+    __shared__ unsigned int s_stop;
+    // one read of the status for the whole block (the block's barriers need
+    // every thread; another block may set the overflow bit meanwhile)
+    if (threadIdx.x == 0) s_stop = *P.status & (kRetryBits | ST_BIN_OVERFLOW);
+    __syncthreads();
+    if (s_stop) return;
     const uint64_t n = *P.prim_total;
-    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n; p += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t cnt = P.pnb[p];
-        if (cnt == 0) continue;
-        const uint64_t base = P.prs[p];
-        if (base + cnt > P.cap) {
-            atomicOr(P.status, ST_BIN_OVERFLOW);
-            continue;
-        }
-        uint32_t lo = 0, hi = P.nitems - 1;  // the draw holding primitive p
-        while (lo < hi) {
-            const uint32_t mid = (lo + hi + 1) >> 1;
-            if (P.iout[mid].prim_start <= p) lo = mid;
-            else hi = mid - 1;
-        }
-        const ItemView& I = P.items[lo];
-        const BandGeom G{I.W, I.H, I.R, I.nbands};
-        const PBox bx = P.pbox[p];
-        uint32_t bl, bh;
-        if (!prim_bands(G, bx, bl, bh)) continue;
-        const RPrim& R = P.prims[p];
-        double w0 = R.w0, w1 = R.w1, w2 = R.w2;
-        int64_t cur = bx.y0;
-        for (uint32_t b = bl; b <= bh && b - bl < cnt; b++) {
-            int64_t a = (int64_t)b * I.R - floordiv_w(bx.x1, I.W);
-            if (a < bx.y0) a = bx.y0;
-            const int64_t gap = a - cur;
-            if (gap > 64) {
-                w0 = repeat_add(w0, R.b0, (uint64_t)gap);
-                w1 = repeat_add(w1, R.b1, (uint64_t)gap);
-                w2 = repeat_add(w2, R.b2, (uint64_t)gap);
-            } else {
-                for (int64_t j = 0; j < gap; j++) {
-                    w0 = __dadd_rn(w0, R.b0);
-                    w1 = __dadd_rn(w1, R.b1);
-                    w2 = __dadd_rn(w2, R.b2);
-                }
+    for (uint64_t t0 = (uint64_t)blockIdx.x * 256; t0 < n; t0 += (uint64_t)gridDim.x * 256) {
+        const uint64_t p0 = t0 + threadIdx.x;
+        const uint32_t cnt0 = p0 < n ? P.pnb[p0] : 0u;
+        uint64_t total;
+        const uint64_t first = block_exclusive_scan<256>((cnt0 + kRowSeg - 1) / kRowSeg, s_warp, &total);
+        s_seg[threadIdx.x] = (uint32_t)first;
+        __syncthreads();
+        for (uint32_t sg = threadIdx.x; sg < (uint32_t)total; sg += blockDim.x) {
+            // the primitive holding segment sg: the last one starting at or before it
+            uint32_t lo = 0, hi = 255;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi + 1) >> 1;
+                if (s_seg[mid] <= sg) lo = mid;
+                else hi = mid - 1;
             }
-            if (gap > 0) cur = a;
-            double* o = P.rstart + 3 * (base + (b - bl));
-            o[0] = w0;
-            o[1] = w1;
-            o[2] = w2;
+            const uint64_t p = t0 + lo;
+            const uint32_t cnt = P.pnb[p];
+            const uint32_t j0 = (sg - s_seg[lo]) * kRowSeg;  // the segment's first band (relative)
+            const uint64_t base = P.prs[p];
+            if (base + cnt > P.cap) {
+                atomicOr(P.status, ST_BIN_OVERFLOW);
+                continue;
+            }
+            uint32_t ilo = 0, ihi = P.nitems - 1;  // the draw holding primitive p
+            while (ilo < ihi) {
+                const uint32_t mid = (ilo + ihi + 1) >> 1;
+                if (P.iout[mid].prim_start <= p) ilo = mid;
+                else ihi = mid - 1;
+            }
+            const ItemView& I = P.items[ilo];
+            const BandGeom G{I.W, I.H, I.R, I.nbands};
+            const PBox bx = P.pbox[p];
+            uint32_t bl, bh;
+            if (!prim_bands(G, bx, bl, bh)) continue;
+            const RPrim& R = P.prims[p];
+            double w0 = R.w0, w1 = R.w1, w2 = R.w2;
+            int64_t cur = bx.y0;
+            const uint32_t jend = min(cnt, j0 + kRowSeg);
+            for (uint32_t j = j0; j < jend && bl + j <= bh; j++) {
+                const uint32_t b = bl + j;
+                int64_t a = (int64_t)b * I.R - floordiv_w(bx.x1, I.W);
+                if (a < bx.y0) a = bx.y0;
+                const int64_t gap = a - cur;
+                if (gap > 0) {
+                    w0 = row_advance(w0, R.b0, gap);
+                    w1 = row_advance(w1, R.b1, gap);
+                    w2 = row_advance(w2, R.b2, gap);
+                    cur = a;
+                }
+                double* o = P.rstart + 3 * (base + j);
+                o[0] = w0;
+                o[1] = w1;
+                o[2] = w2;
+            }
         }
+        __syncthreads();
     }
 }
 
